@@ -1,0 +1,314 @@
+/*
+ * atag.h — C ABI of the GB300 AprilTag quad-detection path.
+ *
+ * Every entry point is stream-ordered: it enqueues work on `stream` and
+ * returns without waiting for the device, unless its comment says it
+ * synchronises.  All pointers named d_* are device pointers; h_* are host
+ * pointers.  No entry point allocates device memory except
+ * atag_detector_create when it is given no workspace.
+ *
+ * The record structs below are layout-identical to the reference's records
+ * (include/boundary_point.h, include/cluster_bounds.h,
+ * include/line_fit_point.h, include/fit_quad.h of the reference project), so
+ * dumps of either side compare byte for byte.
+ *
+ * Constraints shared with the reference (notes.txt:11-16):
+ *   width and height after decimation are multiples of 4, at most 4096
+ *   (14-bit packed coordinates, include/boundary_point.h:20).
+ */
+#ifndef ATAG_H
+#define ATAG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Opaque CUDA stream handle; binary-compatible with cudaStream_t. */
+typedef struct CUstream_st *atag_stream_t;
+
+/* ------------------------------------------------------------------ */
+/* Status codes.  The reference has no error reporting at all.        */
+/* ------------------------------------------------------------------ */
+typedef enum atag_status {
+    ATAG_OK = 0,
+    ATAG_ERR_INVALID_ARGUMENT = 1, /* bad dimensions, null pointer, size  */
+    ATAG_ERR_CUDA = 2,             /* a CUDA runtime call failed          */
+    ATAG_ERR_CAPACITY = 3,         /* a device-side capacity overflowed   */
+    ATAG_ERR_ITERATION_CAP = 4,    /* a bounded union-find loop gave up   */
+    ATAG_ERR_NO_DEVICE = 5,        /* no CUDA device / wrong architecture */
+    ATAG_ERR_OUT_OF_MEMORY = 6     /* workspace too small / cudaMalloc    */
+} atag_status;
+
+/* Device-side status word bits (atag_frame_stats.status). */
+#define ATAG_DEVFLAG_POINT_OVERFLOW 0x1u   /* more boundary points than capacity */
+#define ATAG_DEVFLAG_PAIR_OVERFLOW 0x2u    /* pair hash table full               */
+#define ATAG_DEVFLAG_CLUSTER_OVERFLOW 0x4u /* more filtered clusters than cap    */
+#define ATAG_DEVFLAG_UF_ITERATION_CAP 0x8u /* union-find merge loop cap hit      */
+#define ATAG_DEVFLAG_QUAD_OVERFLOW 0x10u   /* more quads than output capacity    */
+#define ATAG_DEVFLAG_SORT_OVERFLOW 0x20u   /* cluster larger than sort capacity  */
+
+/* ------------------------------------------------------------------ */
+/* Records (layout-identical to the reference).                       */
+/* ------------------------------------------------------------------ */
+
+/* BoundaryPoint, include/boundary_point.h:32-96.
+ * packed_x = [HALF_PIXEL:2 | VALUE:14], packed_y = [COLOR_DIR:1 | 0:1 | VALUE:14] */
+typedef struct atag_boundary_point {
+    uint16_t packed_x;
+    uint16_t packed_y;
+} atag_boundary_point;
+
+/* ClusterPoint, include/boundary_point.h:100-149 (slope = calc_theta). */
+typedef struct atag_cluster_point {
+    uint16_t packed_x;
+    uint16_t packed_y;
+    float slope;
+} atag_cluster_point;
+
+/* ClusterExtents, include/cluster_bounds.h:9-12. */
+typedef struct atag_cluster_extents {
+    uint32_t start;
+    uint32_t count;
+} atag_cluster_extents;
+
+/* ClusterBounds, include/cluster_bounds.h:14-67 (coordinates are 2x). */
+typedef struct atag_cluster_bounds {
+    uint16_t x_min, x_max, y_min, y_max;
+    int32_t gx_sum, gy_sum;
+    int64_t pxgx_pygy_sum;
+    uint32_t start, count;
+} atag_cluster_bounds;
+
+/* LineFitPoint, include/line_fit_point.h:11-48 (a, b unused). */
+typedef struct atag_line_fit_point {
+    int64_t Mx, My, Mxx, Myy, Mxy, W, a, b;
+} atag_line_fit_point;
+
+/* PeakExtents, include/fit_quad.h:9-12. */
+typedef struct atag_peak_extents {
+    uint32_t start;
+    uint32_t count;
+} atag_peak_extents;
+
+/* Corner, include/fit_quad.h:21-25. */
+typedef struct atag_corner {
+    uint32_t line_fit_point_index;
+    uint16_t cluster_index;
+    float error;
+} atag_corner;
+
+/* FittedQuad, include/fit_quad.h:27-31. */
+typedef struct atag_fitted_quad {
+    atag_line_fit_point moments[4];
+    uint16_t num_in_moments[4];
+    uint16_t indices[4];
+} atag_fitted_quad;
+
+/* QuadCorners, include/fit_quad.h:33-37.  blob_index is left unset by the
+ * reference; here it holds the index of the FittedQuad it came from. */
+typedef struct atag_quad_corners {
+    float corners[4][2];
+    uint8_t reversed_border;
+    uint8_t pad_[3];
+    uint32_t blob_index;
+} atag_quad_corners;
+
+/* ------------------------------------------------------------------ */
+/* Configuration: every constant the reference hard-codes.  Defaults  */
+/* (atag_config_default) reproduce the reference.                     */
+/* ------------------------------------------------------------------ */
+typedef struct atag_config {
+    int32_t decimate;              /* point-sampling factor (>=1); reference: absent (1) */
+    int32_t min_white_black_diff;  /* threshold.cpp:86: "max-min < 5" -> 127            */
+    int32_t min_component_size;    /* find_boundaries.cpp:82,98,143: sizes >= 25         */
+    int32_t min_cluster_pixels;    /* cluster_bounds.h:89: 5 (and the fixed 24 gate)     */
+    int32_t tag_width;             /* cluster_bounds.h:86: bbox area gate (2x coords)    */
+    int32_t normal_border;         /* cluster_bounds.h:87                                */
+    int32_t reversed_border;       /* cluster_bounds.h:88                                */
+    float max_line_fit_mse;        /* fit_quad.cpp:7                                     */
+    float critical_angle_deg;      /* 10: cos() of it is taken in double, then rounded to
+                                      float for do_indexing (fit_quad.cpp:399) and kept
+                                      double for the corner check (main.cpp:1039)     */
+    int32_t min_tag_width;         /* main.cpp:1037: area >= 0.95 * w^2                  */
+    int32_t compat_peak_index;     /* 1: index cluster extents by peak-cluster position
+                                      exactly like fit_quad.cpp:405-408 (default);
+                                      0: index by the corner's own cluster             */
+} atag_config;
+
+void atag_config_default(atag_config *cfg);
+
+/* Per-frame counters written by the device (one struct per frame). */
+typedef struct atag_frame_stats {
+    uint32_t width, height;      /* after decimation                       */
+    uint32_t n_points;           /* P   boundary points (after size gate)  */
+    uint32_t n_pairs;            /* C   distinct cluster pairs             */
+    uint32_t n_clusters;         /* C_f clusters passing ValidBlobFilter   */
+    uint32_t n_cluster_points;   /* P_f points in those clusters           */
+    uint32_t n_corners;          /* K   corner peaks                       */
+    uint32_t n_peak_clusters;    /* C_p clusters with >= 1 peak            */
+    uint32_t n_fitted;           /* FittedQuads written (nonzero indices)  */
+    uint32_t n_quads;            /* Q   quads after geometric rejection    */
+    uint32_t status;             /* ATAG_DEVFLAG_* bits                    */
+    uint32_t reserved[5];
+} atag_frame_stats;
+
+/* ------------------------------------------------------------------ */
+/* Library                                                            */
+/* ------------------------------------------------------------------ */
+const char *atag_status_string(atag_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char *atag_last_error(void);
+/* Checks for an sm_103 device and loads the kernels.  Idempotent. */
+atag_status atag_init(void);
+/* Number of kernel launches this library has issued since load (all streams). */
+uint64_t atag_launch_count(void);
+
+/* ------------------------------------------------------------------ */
+/* Stage entry points: drop-ins for the reference's device functions. */
+/* ------------------------------------------------------------------ */
+
+/* Point-sampling decimation dst(x,y) = src(f*x, f*y); dst is
+ * (src_w/f) x (src_h/f).  The reference has none (notes.txt:18-21). */
+atag_status atag_decimate(const uint8_t *d_src, size_t src_width, size_t src_height,
+                          size_t factor, uint8_t *d_dst, atag_stream_t stream);
+
+/* Replaces threshold_image (include/threshold.h:6-10, src/threshold.cpp:3-98).
+ * d_extrema / d_filtered_extrema are 2 bytes per 4x4 tile (min, max) and may
+ * be NULL: the fused kernel keeps them in shared memory and only writes them
+ * when asked. */
+atag_status atag_threshold_image(const uint8_t *d_grayscale, uint8_t *d_extrema,
+                                 uint8_t *d_filtered_extrema, uint8_t *d_thresholded,
+                                 size_t width, size_t height, atag_stream_t stream);
+
+/* Replaces image_segmentation (include/segmentation.h:11-15,
+ * src/segmentation.cpp:95-392).  labels: u32 per pixel, bit 31 = white,
+ * low 31 bits = min slot index of the component (255: even slot y*w+x of the
+ * 2x2 block, 0: odd slot), 127 -> 0.  sizes: u32[width*height], pixel count
+ * of each component at its root index, 0 elsewhere.  label_scratch:
+ * u32[width*height] union-find forest.  sizes_elem is unused, as in the
+ * reference. */
+atag_status atag_image_segmentation(const uint8_t *d_thresholded, uint32_t *d_label_scratch,
+                                    uint32_t *d_labels, uint32_t *d_sizes, size_t sizes_elem,
+                                    size_t width, size_t height, atag_stream_t stream);
+
+/* Replaces find_boundaries (include/find_boundaries.h:8-12,
+ * src/find_boundaries.cpp:10-155): the dense 4-plane output at
+ * plane*w*h + y*w + x.  The caller pre-fills points with 0 and blob_labels
+ * with 0xFF, as src/main.cpp:312-315 does. */
+atag_status atag_find_boundaries(const uint32_t *d_labels, const uint32_t *d_sizes,
+                                 atag_boundary_point *d_points, uint64_t *d_blob_labels,
+                                 size_t width, size_t height, atag_stream_t stream);
+
+/* Replaces fit_lines (include/fit_quad.h:46-49, src/fit_quad.cpp:153-375).
+ * points: per-cluster inclusive prefix sums of line-fit moments.  The
+ * caller pre-zeroes found_corners (src/main.cpp:316-317).  Unlike the
+ * reference this does not block the host. */
+atag_status atag_fit_lines(const atag_line_fit_point *d_points, const uint16_t *d_cluster_indices,
+                           const atag_cluster_extents *d_cluster_extents, size_t points_size,
+                           atag_corner *d_found_corners, atag_stream_t stream);
+
+/* Replaces do_indexing (include/fit_quad.h:51-55, src/fit_quad.cpp:392-535),
+ * including its cluster_extents[peak position] indexing.  The caller
+ * pre-zeroes fitted (src/main.cpp:318-319).  Does not block the host. */
+atag_status atag_do_indexing(const atag_peak_extents *d_extents, size_t extents_count,
+                             const atag_corner *d_compacted_corners,
+                             const atag_line_fit_point *d_points,
+                             const atag_cluster_extents *d_cluster_extents,
+                             atag_fitted_quad *d_fitted, atag_stream_t stream);
+
+/* Replaces the host function process_fitted_quads (src/main.cpp:1035-1162)
+ * up to, not including, tag decoding: refit the four lines, intersect them
+ * in FP64, reject by area and angle.  Runs on the device; quads whose four
+ * indices are zero are skipped.  *d_count receives the number written. */
+atag_status atag_process_fitted_quads(const atag_fitted_quad *d_fitted, size_t fitted_count,
+                                      size_t width, size_t height, const atag_config *cfg,
+                                      atag_quad_corners *d_quads, size_t quads_capacity,
+                                      uint32_t *d_count, atag_stream_t stream);
+
+/* ------------------------------------------------------------------ */
+/* Whole-path detector (replaces src/main.cpp:322-1024 stages 1-16 and */
+/* the corner intersection).                                          */
+/* ------------------------------------------------------------------ */
+typedef struct atag_detector atag_detector;
+
+/* One frame of a batch.  d_grey is the source image before decimation. */
+typedef struct atag_frame {
+    const uint8_t *d_grey;
+    uint32_t src_width, src_height;
+} atag_frame;
+
+/* Bytes of device workspace a detector needs for up to max_frames frames
+ * whose decimated sizes sum to at most max_total_pixels (and none exceeds
+ * max_width x max_height after decimation). */
+atag_status atag_workspace_size(const atag_config *cfg, size_t max_width, size_t max_height,
+                                size_t max_frames, size_t max_total_pixels, size_t *bytes);
+
+/* Creates a detector.  If d_workspace is NULL the detector allocates (and
+ * later frees) its own workspace of atag_workspace_size bytes; otherwise the
+ * caller's buffer of at least that size is used and nothing is allocated. */
+atag_status atag_detector_create(const atag_config *cfg, size_t max_width, size_t max_height,
+                                 size_t max_frames, size_t max_total_pixels, void *d_workspace,
+                                 size_t workspace_bytes, atag_detector **out);
+atag_status atag_detector_destroy(atag_detector *det);
+
+/* Detects quads in n frames at once.  Writes up to quads_capacity quads per
+ * frame to d_quads + f*quads_capacity and the frame's counters to
+ * d_stats[f].  Stream-ordered, no host synchronisation: every stage sizes
+ * its grid from upper bounds and reads its counts on the device, so the
+ * call can be captured in a CUDA graph. */
+atag_status atag_detect_batch(atag_detector *det, const atag_frame *h_frames, size_t n_frames,
+                              atag_quad_corners *d_quads, size_t quads_capacity,
+                              atag_frame_stats *d_stats, atag_stream_t stream);
+
+/* Single frame convenience form of atag_detect_batch. */
+atag_status atag_detect(atag_detector *det, const uint8_t *d_grey, size_t src_width,
+                        size_t src_height, atag_quad_corners *d_quads, size_t quads_capacity,
+                        atag_frame_stats *d_stats, atag_stream_t stream);
+
+/* Host-buffer form: copies h_grey to the device, detects, copies the quads
+ * and counters back and synchronises the stream.  *h_n_quads receives the
+ * quad count (quads beyond quads_capacity are dropped and flagged). */
+atag_status atag_detect_host(atag_detector *det, const uint8_t *h_grey, size_t src_width,
+                             size_t src_height, atag_quad_corners *h_quads,
+                             size_t quads_capacity, atag_frame_stats *h_stats,
+                             atag_stream_t stream);
+
+/* Intermediate buffers of the last detect call, for parity checks and
+ * debugging.  Pointers are device pointers into the workspace and stay
+ * valid until the next detect call.  Counts are in atag_frame_stats. */
+typedef struct atag_frame_views {
+    const uint8_t *decimated;                   /* w*h                              */
+    const uint8_t *thresholded;                 /* w*h                              */
+    const uint32_t *labels;                     /* w*h                              */
+    const uint32_t *sizes;                      /* w*h                              */
+    const uint64_t *pair_points;                /* n_points: (pair slot << 32) | packed */
+    const uint64_t *pair_keys;                  /* pair_capacity: slot -> pair key  */
+    uint32_t pair_capacity;
+    uint32_t reserved_;
+    const uint64_t *cluster_keys;               /* n_clusters pair keys, ascending  */
+    const atag_cluster_bounds *cluster_bounds;  /* n_clusters (start = position among
+                                                   all pairs' points in key order)  */
+    const atag_cluster_extents *cluster_extents;/* n_clusters                       */
+    const atag_cluster_point *cluster_points;   /* n_cluster_points, sorted         */
+    const atag_line_fit_point *line_fit_points; /* n_cluster_points prefix sums     */
+    const uint32_t *peak_count;                 /* n_clusters: peaks per cluster    */
+    const atag_corner *peaks;                   /* n_clusters x 10: best peaks      */
+    const uint32_t *peak_clusters;              /* n_peak_clusters: rank -> cluster */
+    const atag_peak_extents *peak_extents;      /* n_peak_clusters                  */
+    const atag_fitted_quad *fitted;             /* n_peak_clusters (by rank)        */
+} atag_frame_views;
+
+/* Selects the CUDA device this library launches on for the calling host
+ * thread (the library keeps its own CUDA runtime state). */
+atag_status atag_use_device(int ordinal);
+
+atag_status atag_detector_views(const atag_detector *det, size_t frame, atag_frame_views *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATAG_H */

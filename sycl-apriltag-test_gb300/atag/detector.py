@@ -1,0 +1,140 @@
+"""Detector: the whole quad-detection path for one frame or a batch of
+frames of mixed sizes, over a workspace that torch allocates once."""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import lib
+from .records import (CLUSTER_BOUNDS, CLUSTER_EXTENTS, CLUSTER_POINT, CORNER, FITTED_QUAD, FRAME_STATS,
+                      LINE_FIT_POINT, PEAK_EXTENTS, QUAD_CORNERS, Frame, FrameViews)
+
+_P = ctypes.c_void_p
+
+
+class Detector:
+    """Wraps atag_detector (include/atag.h).
+
+    max_width/max_height bound a frame after decimation; max_frames and
+    max_total_pixels bound a batch.  `enqueue` is stream-ordered and does not
+    synchronise; `results` copies the quads back.
+    """
+
+    def __init__(self, max_width: int, max_height: int, max_frames: int = 1, max_total_pixels: int = 0,
+                 config=None, quad_capacity: int = 1024):
+        self.L = lib.init()
+        self.cfg = config or lib.default_config()
+        self.max_frames = max_frames
+        self.quad_capacity = quad_capacity
+        size = ctypes.c_size_t()
+        lib.check(self.L.atag_workspace_size(ctypes.byref(self.cfg), max_width, max_height, max_frames,
+                                             max_total_pixels, ctypes.byref(size)), "atag_workspace_size")
+        self.workspace = torch.empty(size.value, dtype=torch.uint8, device="cuda")
+        self.handle = _P()
+        lib.check(self.L.atag_detector_create(ctypes.byref(self.cfg), max_width, max_height, max_frames,
+                                              max_total_pixels, _P(self.workspace.data_ptr()), size.value,
+                                              ctypes.byref(self.handle)), "atag_detector_create")
+        self.d_quads = torch.zeros(max_frames * quad_capacity * QUAD_CORNERS.itemsize, dtype=torch.uint8,
+                                   device="cuda")
+        self.d_stats = torch.zeros(max_frames * FRAME_STATS.itemsize, dtype=torch.uint8, device="cuda")
+        self._frames = []
+        self._n = 0
+
+    def close(self):
+        if self.handle:
+            self.L.atag_detector_destroy(self.handle)
+            self.handle = _P()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def enqueue(self, frames, stream=None):
+        """Launches detection of `frames` (uint8 CUDA tensors, H x W, before
+        decimation) on `stream` (default: torch's current stream)."""
+        frames = [f if f.is_contiguous() else f.contiguous() for f in frames]
+        n = len(frames)
+        arr = (Frame * n)()
+        for i, f in enumerate(frames):
+            assert f.dtype == torch.uint8 and f.is_cuda and f.dim() == 2
+            arr[i].d_grey = f.data_ptr()
+            arr[i].src_width = f.shape[1]
+            arr[i].src_height = f.shape[0]
+        s = stream if stream is not None else torch.cuda.current_stream()
+        lib.check(self.L.atag_detect_batch(self.handle, arr, n, _P(self.d_quads.data_ptr()), self.quad_capacity,
+                                           _P(self.d_stats.data_ptr()), _P(s.cuda_stream)), "atag_detect_batch")
+        self._frames = frames
+        self._n = n
+
+    def stats(self) -> np.ndarray:
+        return self.d_stats[: self._n * FRAME_STATS.itemsize].cpu().numpy().view(FRAME_STATS)
+
+    def results(self):
+        """(list of QUAD_CORNERS arrays, stats array) of the last enqueue."""
+        st = self.stats()
+        q = self.d_quads[: self._n * self.quad_capacity * QUAD_CORNERS.itemsize].cpu().numpy().view(QUAD_CORNERS)
+        q = q.reshape(self._n, self.quad_capacity)
+        return [q[i, : int(st[i]["n_quads"])].copy() for i in range(self._n)], st
+
+    def detect(self, frames):
+        self.enqueue(frames)
+        return self.results()
+
+    def detect_host(self, image: np.ndarray, stream=None):
+        """Host-buffer path: copy in, detect, copy out, synchronise."""
+        img = np.ascontiguousarray(image, dtype=np.uint8)
+        cap = min(self.quad_capacity, 4096)
+        out = np.zeros(cap, QUAD_CORNERS)
+        st = np.zeros(1, FRAME_STATS)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        lib.check(self.L.atag_detect_host(self.handle, _P(img.ctypes.data), img.shape[1], img.shape[0],
+                                          _P(out.ctypes.data), cap, _P(st.ctypes.data), _P(s.cuda_stream)),
+                  "atag_detect_host")
+        return out[: int(st[0]["n_quads"])], st[0]
+
+    # -- intermediates -------------------------------------------------------
+    def _dev_bytes(self, ptr, nbytes):
+        if nbytes == 0 or not ptr:
+            return np.zeros(0, np.uint8)
+        base = self.workspace.data_ptr()
+        if base <= ptr < base + self.workspace.numel():
+            off = ptr - base
+            return self.workspace[off: off + nbytes].cpu().numpy()
+        for f in self._frames:
+            if f.data_ptr() <= ptr < f.data_ptr() + f.numel():
+                off = ptr - f.data_ptr()
+                return f.reshape(-1)[off: off + nbytes].cpu().numpy()
+        raise ValueError("pointer outside the workspace")
+
+    def views(self, i: int = 0) -> dict:
+        """Copies frame i's intermediates to the host (numpy records)."""
+        v = FrameViews()
+        lib.check(self.L.atag_detector_views(self.handle, i, ctypes.byref(v)), "atag_detector_views")
+        st = self.stats()[i]
+        w, h = int(st["width"]), int(st["height"])
+        N = w * h
+        ncl, npf, ncp = int(st["n_clusters"]), int(st["n_cluster_points"]), int(st["n_peak_clusters"])
+        npts = int(st["n_points"])
+        g = self._dev_bytes
+        return {
+            "stats": st,
+            "decimated": g(v.decimated, N).reshape(h, w),
+            "thresholded": g(v.thresholded, N).reshape(h, w),
+            "labels": g(v.labels, 4 * N).view(np.uint32).reshape(h, w),
+            "sizes": g(v.sizes, 4 * N).view(np.uint32),
+            "pair_points": g(v.pair_points, 8 * npts).view(np.uint64),
+            "pair_keys": g(v.pair_keys, 8 * v.pair_capacity).view(np.uint64),
+            "cluster_keys": g(v.cluster_keys, 8 * ncl).view(np.uint64),
+            "cluster_bounds": g(v.cluster_bounds, 32 * ncl).view(CLUSTER_BOUNDS),
+            "cluster_extents": g(v.cluster_extents, 8 * ncl).view(CLUSTER_EXTENTS),
+            "cluster_points": g(v.cluster_points, 8 * npf).view(CLUSTER_POINT),
+            "line_fit": g(v.line_fit_points, 64 * npf).view(LINE_FIT_POINT),
+            "peak_count": g(v.peak_count, 4 * ncl).view(np.uint32),
+            "peaks": g(v.peaks, CORNER.itemsize * 10 * ncl).view(CORNER).reshape(ncl, 10) if ncl else
+            np.zeros((0, 10), CORNER),
+            "peak_clusters": g(v.peak_clusters, 4 * ncp).view(np.uint32),
+            "peak_extents": g(v.peak_extents, 8 * ncp).view(PEAK_EXTENTS),
+            "fitted": g(v.fitted, FITTED_QUAD.itemsize * ncp).view(FITTED_QUAD),
+        }

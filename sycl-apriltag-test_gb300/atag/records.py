@@ -1,0 +1,59 @@
+"""numpy mirrors of the C records in include/atag.h (layout-identical to the
+reference's BoundaryPoint, ClusterPoint, ClusterBounds, LineFitPoint,
+Corner, FittedQuad, QuadCorners)."""
+import ctypes
+
+import numpy as np
+
+BOUNDARY_POINT = np.dtype([("packed_x", "<u2"), ("packed_y", "<u2")])
+CLUSTER_POINT = np.dtype([("packed_x", "<u2"), ("packed_y", "<u2"), ("slope", "<f4")])
+CLUSTER_EXTENTS = np.dtype([("start", "<u4"), ("count", "<u4")])
+PEAK_EXTENTS = CLUSTER_EXTENTS
+CLUSTER_BOUNDS = np.dtype([("x_min", "<u2"), ("x_max", "<u2"), ("y_min", "<u2"), ("y_max", "<u2"),
+                           ("gx_sum", "<i4"), ("gy_sum", "<i4"), ("pxgx_pygy_sum", "<i8"),
+                           ("start", "<u4"), ("count", "<u4")])
+LINE_FIT_POINT = np.dtype([(n, "<i8") for n in ("Mx", "My", "Mxx", "Myy", "Mxy", "W", "a", "b")])
+CORNER = np.dtype({"names": ["line_fit_point_index", "cluster_index", "error"],
+                   "formats": ["<u4", "<u2", "<f4"], "offsets": [0, 4, 8], "itemsize": 12})
+FITTED_QUAD = np.dtype([("moments", LINE_FIT_POINT, (4,)), ("num_in_moments", "<u2", (4,)),
+                        ("indices", "<u2", (4,))])
+QUAD_CORNERS = np.dtype([("corners", "<f4", (4, 2)), ("reversed_border", "u1"), ("pad_", "u1", (3,)),
+                         ("blob_index", "<u4")])
+FRAME_STATS = np.dtype([(n, "<u4") for n in ("width", "height", "n_points", "n_pairs", "n_clusters",
+                                              "n_cluster_points", "n_corners", "n_peak_clusters",
+                                              "n_fitted", "n_quads", "status")] + [("reserved", "<u4", (5,))])
+
+assert BOUNDARY_POINT.itemsize == 4 and CLUSTER_POINT.itemsize == 8 and CLUSTER_EXTENTS.itemsize == 8
+assert CLUSTER_BOUNDS.itemsize == 32 and LINE_FIT_POINT.itemsize == 64 and CORNER.itemsize == 12
+assert FITTED_QUAD.itemsize == 272 and QUAD_CORNERS.itemsize == 40 and FRAME_STATS.itemsize == 64
+
+
+class Config(ctypes.Structure):
+    """atag_config; field order and types follow include/atag.h."""
+    _fields_ = [("decimate", ctypes.c_int32), ("min_white_black_diff", ctypes.c_int32),
+                ("min_component_size", ctypes.c_int32), ("min_cluster_pixels", ctypes.c_int32),
+                ("tag_width", ctypes.c_int32), ("normal_border", ctypes.c_int32),
+                ("reversed_border", ctypes.c_int32), ("max_line_fit_mse", ctypes.c_float),
+                ("critical_angle_deg", ctypes.c_float), ("min_tag_width", ctypes.c_int32),
+                ("compat_peak_index", ctypes.c_int32)]
+
+
+class Frame(ctypes.Structure):
+    _fields_ = [("d_grey", ctypes.c_void_p), ("src_width", ctypes.c_uint32), ("src_height", ctypes.c_uint32)]
+
+
+class FrameViews(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("decimated", "thresholded", "labels", "sizes", "pair_points",
+                                                "pair_keys")] + \
+               [("pair_capacity", ctypes.c_uint32), ("reserved_", ctypes.c_uint32)] + \
+               [(n, ctypes.c_void_p) for n in ("cluster_keys", "cluster_bounds", "cluster_extents",
+                                                "cluster_points", "line_fit_points", "peak_count", "peaks",
+                                                "peak_clusters", "peak_extents", "fitted")]
+
+# device flag bits (atag_frame_stats.status)
+DEVFLAG_POINT_OVERFLOW = 0x1
+DEVFLAG_PAIR_OVERFLOW = 0x2
+DEVFLAG_CLUSTER_OVERFLOW = 0x4
+DEVFLAG_UF_ITERATION_CAP = 0x8
+DEVFLAG_QUAD_OVERFLOW = 0x10
+DEVFLAG_SORT_OVERFLOW = 0x20

@@ -1,0 +1,392 @@
+// atag_device.cuh — device-side arithmetic shared by every kernel.
+//
+// Each float/double operation is spelled with an explicit round-to-nearest
+// intrinsic (__fadd_rn, __fmul_rn, __fdiv_rn, __dsqrt_rn, ...) so that nvcc
+// can neither contract a multiply-add into an FMA nor pick an approximate
+// division: the results are the IEEE results of the operations as written in
+// the reference (C++ semantics, one rounding per operation).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/atag.h"
+
+namespace atag {
+
+constexpr uint32_t LABEL_PIXEL_MASK = 0x80000000u;  // segmentation.h:7
+constexpr uint32_t LABEL_VALUE_MASK = 0x7FFFFFFFu;  // segmentation.h:9
+constexpr uint16_t COLOR_DIR_MASK = 0x8000u;        // boundary_point.h:18
+constexpr uint16_t COORD_VALUE_MASK = 0x3FFFu;      // boundary_point.h:20
+constexpr uint32_t INVALID = 0xFFFFFFFFu;
+
+// ---------------------------------------------------------------------------
+// Wrapping int64 arithmetic (the reference's int64 products may overflow at
+// 4K; two's-complement wrap is what the hardware does).
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ long long wmul(long long a, long long b) {
+    return (long long)((unsigned long long)a * (unsigned long long)b);
+}
+__host__ __device__ __forceinline__ long long wadd(long long a, long long b) {
+    return (long long)((unsigned long long)a + (unsigned long long)b);
+}
+__host__ __device__ __forceinline__ long long wsub(long long a, long long b) {
+    return (long long)((unsigned long long)a - (unsigned long long)b);
+}
+
+// hypotf as sqrt of the exactly-formed squares summed in double, rounded
+// once to float.
+__device__ __forceinline__ float hypot_f(float a, float b) {
+    double da = (double)a, db = (double)b;
+    return __double2float_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(da, da), __dmul_rn(db, db))));
+}
+
+// ---------------------------------------------------------------------------
+// BoundaryPoint helpers (boundary_point.h).  COORDINATE_HALF_PIXEL_MASK is 0
+// (boundary_point.h:16), so dx() == 1 and dy() == 0 for every point.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint32_t bp_xd(uint32_t packed) {  // x_with_dx()
+    return (2u * (packed & COORD_VALUE_MASK) + 1u) & 0xFFFFu;
+}
+__host__ __device__ __forceinline__ uint32_t bp_yd(uint32_t packed) {  // y_with_dy()
+    return (2u * ((packed >> 16) & COORD_VALUE_MASK)) & 0xFFFFu;
+}
+__host__ __device__ __forceinline__ int bp_gx(uint32_t packed) {
+    return ((packed >> 16) & COLOR_DIR_MASK) ? 1 : -1;
+}
+__host__ __device__ __forceinline__ int bp_gy(uint32_t) { return 0; }
+
+// calc_theta, boundary_point.h:48-61
+__device__ __forceinline__ float calc_theta(uint32_t packed, float cx, float cy) {
+    float dx = __fsub_rn((float)bp_xd(packed), cx);
+    float dy = __fsub_rn((float)bp_yd(packed), cy);
+    float quadrant;
+    if (dx > 0) quadrant = dy > 0 ? 65536.0f : 0.0f;
+    else quadrant = dy > 0 ? 131072.0f : -65536.0f;
+    if ((dx > 0) == (dy > 0)) return __fadd_rn(quadrant, __fdiv_rn(dy, dx));
+    return __fsub_rn(quadrant, __fdiv_rn(dx, dy));
+}
+
+// ClusterBounds::cx/cy, cluster_bounds.h:47-49
+__device__ __forceinline__ float bounds_cx(uint32_t xmin, uint32_t xmax) {
+    float h = __fmul_rn((float)(xmin + xmax), 0.5f);
+    return __double2float_rn(__dadd_rn((double)h, 0.05118));
+}
+__device__ __forceinline__ float bounds_cy(uint32_t ymin, uint32_t ymax) {
+    float h = __fmul_rn((float)(ymin + ymax), 0.5f);
+    return __double2float_rn(__dadd_rn((double)h, -0.028581));
+}
+// ClusterBounds::dot, cluster_bounds.h:51-66
+__device__ __forceinline__ float bounds_dot(uint32_t xmin, uint32_t xmax, uint32_t ymin, uint32_t ymax,
+                                            int gx_sum, int gy_sum, long long pxgx) {
+    uint32_t sx = xmin + xmax, sy = ymin + ymax;
+    int t = (int)(sx * (uint32_t)gx_sum + sy * (uint32_t)gy_sum);
+    float cxcy = __double2float_rn(__dmul_rn((double)t, 0.5));
+    float gxc = __double2float_rn(__dmul_rn(0.05118, (double)__int2float_rn(gx_sum)));
+    float gyc = __double2float_rn(__dmul_rn(-0.028581, (double)__int2float_rn(gy_sum)));
+    float r = __fmul_rn(2.0f, __ll2float_rn(pxgx));
+    r = __fsub_rn(r, cxcy);
+    r = __fsub_rn(r, gxc);
+    r = __fsub_rn(r, gyc);
+    return r;
+}
+
+// ValidBlobFilter, cluster_bounds.h:85-120
+struct FilterParams {
+    uint32_t min_cluster_pixels;
+    uint32_t max_cluster_pixels;  // 2 * (2 w + 2 h)
+    uint32_t tag_width;
+    int normal_border, reversed_border;
+};
+__device__ __forceinline__ bool valid_blob(const FilterParams& f, uint32_t count, uint32_t xmin,
+                                           uint32_t xmax, uint32_t ymin, uint32_t ymax, int gx_sum,
+                                           int gy_sum, long long pxgx) {
+    if (count < f.min_cluster_pixels) return false;
+    if (count < 24) return false;
+    if (count > f.max_cluster_pixels) return false;
+    if ((uint32_t)((int)(xmax - xmin) * (int)(ymax - ymin)) < f.tag_width) return false;
+    bool reversed = bounds_dot(xmin, xmax, ymin, ymax, gx_sum, gy_sum, pxgx) < 0.0f;
+    if (!f.reversed_border && reversed) return false;
+    if (!f.normal_border && !reversed) return false;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Line-fit moments (line_fit_point.h, fit_quad.cpp:15-105)
+// ---------------------------------------------------------------------------
+struct Moment {
+    long long Mx, My, Mxx, Myy, Mxy, W;
+};
+
+__device__ __forceinline__ Moment load_moment(const atag_line_fit_point* p) {
+    const longlong2* q = reinterpret_cast<const longlong2*>(p);
+    longlong2 a = q[0], b = q[1], c = q[2];
+    return Moment{a.x, a.y, b.x, b.y, c.x, c.y};
+}
+__device__ __forceinline__ void store_moment(atag_line_fit_point* p, const Moment& m) {
+    longlong2* q = reinterpret_cast<longlong2*>(p);
+    q[0] = make_longlong2(m.Mx, m.My);
+    q[1] = make_longlong2(m.Mxx, m.Myy);
+    q[2] = make_longlong2(m.Mxy, m.W);
+    q[3] = make_longlong2(0, 0);
+}
+__device__ __forceinline__ Moment m_add(Moment a, const Moment& b) {
+    a.Mx = wadd(a.Mx, b.Mx); a.My = wadd(a.My, b.My); a.Mxx = wadd(a.Mxx, b.Mxx);
+    a.Myy = wadd(a.Myy, b.Myy); a.Mxy = wadd(a.Mxy, b.Mxy); a.W = wadd(a.W, b.W);
+    return a;
+}
+__device__ __forceinline__ Moment m_sub(Moment a, const Moment& b) {
+    a.Mx = wsub(a.Mx, b.Mx); a.My = wsub(a.My, b.My); a.Mxx = wsub(a.Mxx, b.Mxx);
+    a.Myy = wsub(a.Myy, b.Myy); a.Mxy = wsub(a.Mxy, b.Mxy); a.W = wsub(a.W, b.W);
+    return a;
+}
+
+// Integer floor(sqrt(v)) for v < 2^17: equals (int64)hypotf(gx, gy) for the
+// central differences of a u8 image (line_fit_point.h:70-75).
+__device__ __forceinline__ uint32_t isqrt_small(uint32_t v) {
+    uint32_t r = (uint32_t)__fsqrt_rn((float)v);
+    while (r * r > v) r--;
+    while ((r + 1) * (r + 1) <= v) r++;
+    return r;
+}
+
+// compute_initial_linefit, line_fit_point.h:50-86 (weight row rx/2, sic).
+__device__ __forceinline__ Moment initial_linefit(uint32_t packed, uint32_t width, uint32_t height,
+                                                  const uint8_t* __restrict__ grey) {
+    long long rx = (long long)bp_xd(packed) + 1;
+    long long ry = (long long)bp_yd(packed) + 1;
+    uint32_t x = (uint32_t)(rx / 2);
+    uint32_t y = (uint32_t)(rx / 2);
+    long long W = 1;
+    if (x > 0 && x + 1 < width && y > 0 && y + 1 < height) {
+        int gx = (int)__ldg(grey + (size_t)y * width + x + 1) - (int)__ldg(grey + (size_t)y * width + x - 1);
+        int gy = (int)__ldg(grey + (size_t)(y + 1) * width + x) - (int)__ldg(grey + (size_t)(y - 1) * width + x);
+        W += (long long)isqrt_small((uint32_t)(gx * gx + gy * gy));
+    }
+    return Moment{W * rx, W * ry, W * rx * rx, W * ry * ry, W * rx * ry, W};
+}
+
+// get_moment, fit_quad.cpp:15-35 over a prefix-sum array of one cluster.
+__device__ __forceinline__ Moment get_moment(const atag_line_fit_point* points, unsigned long long n,
+                                             unsigned long long i0, unsigned long long i1,
+                                             unsigned long long* total) {
+    Moment r{0, 0, 0, 0, 0, 0};
+    *total = 0;
+    if (i0 < i1) {
+        *total = i1 - i0 + 1;
+        r = load_moment(points + i1);
+        if (i0 > 0) r = m_sub(r, load_moment(points + i0 - 1));
+    } else if (i1 < i0) {
+        *total = n - i0 + i1 + 1;
+        r = load_moment(points + (n - 1));
+        r = m_sub(r, load_moment(points + i0 - 1));
+        r = m_add(r, load_moment(points + i1));
+    }
+    return r;
+}
+
+// fit_line, fit_quad.cpp:37-105.
+__device__ __forceinline__ void fit_line(const Moment& m, unsigned long long num_in_moment, float* lp,
+                                         float* err, float* mse) {
+    long long Csxx = wsub(wmul(m.Mxx, m.W), wmul(m.Mx, m.Mx));
+    long long Csxy = wsub(wmul(m.Mxy, m.W), wmul(m.Mx, m.My));
+    long long Csyy = wsub(wmul(m.Myy, m.W), wmul(m.My, m.My));
+    long long cf = wmul(wmul(m.W, m.W), 4);
+    float sdist = hypot_f(__ll2float_rn(wsub(Csxx, Csyy)), __ll2float_rn(wmul(2, Csxy)));
+    float num = __fsub_rn(__ll2float_rn(wadd(Csxx, Csyy)), sdist);
+    float eig = __fdiv_rn(num, __ll2float_rn(wmul(cf, 2)));
+    if (lp) {
+        float nx1 = __fsub_rn(__ll2float_rn(wsub(Csxx, Csyy)), sdist);
+        float ny1 = __ll2float_rn(wmul(2, Csxy));
+        float nx2 = ny1;
+        float ny2 = __fsub_rn(__ll2float_rn(wsub(Csyy, Csxx)), sdist);
+        float M1 = __fadd_rn(__fmul_rn(nx1, nx1), __fmul_rn(ny1, ny1));
+        float M2 = __fadd_rn(__fmul_rn(nx2, nx2), __fmul_rn(ny2, ny2));
+        float nx, ny;
+        if (M1 > M2) { nx = nx1; ny = ny1; } else { nx = nx2; ny = ny2; }
+        float w2 = __ll2float_rn(wmul(m.W, 2));
+        lp[0] = __fdiv_rn(__ll2float_rn(m.Mx), w2);
+        lp[1] = __fdiv_rn(__ll2float_rn(m.My), w2);
+        float length = hypot_f(nx, ny);
+        if ((double)fabsf(length) < 1e-12) {
+            lp[2] = 0.0f;
+            lp[3] = 0.0f;
+        } else {
+            lp[2] = __fdiv_rn(nx, length);
+            lp[3] = __fdiv_rn(ny, length);
+        }
+    }
+    if (err) *err = __fmul_rn(__ull2float_rn(num_in_moment), eig);
+    if (mse) *mse = eig;
+}
+
+// Error of the window [i-k, i+k] around global point x, fit_quad.cpp:202-225.
+__device__ __forceinline__ float window_error(const atag_line_fit_point* points, uint32_t start,
+                                              uint32_t count, long long x) {
+    unsigned long long k = count / 12;
+    if (k > 20) k = 20;
+    if (k < 2) return __int_as_float(0x7fc00000);
+    unsigned long long i0 = (unsigned long long)((long long)count + x - (long long)start - (long long)k) % count;
+    unsigned long long i1 = (unsigned long long)((long long)count + x - (long long)start + (long long)k) % count;
+    unsigned long long n;
+    Moment m = get_moment(points + start, count, i0, i1, &n);
+    float e;
+    fit_line(m, n, nullptr, &e, nullptr);
+    return e;
+}
+
+// 7-tap low-pass filter, fit_quad.cpp:10-13
+__device__ __forceinline__ float filter_tap(int i) {
+    switch (i) {
+    case 0: case 6: return 0x1.6c0504p-7f;
+    case 1: case 5: return 0x1.152aaap-3f;
+    case 2: case 4: return 0x1.368b3p-1f;
+    default: return 0x1p+0f;
+    }
+}
+
+// Combinatorial number system decode of n < 210 into 4 descending indices
+// below 10 (combinadics.h:36-53 with Combinadics<uint8_t,15,4,16>).
+__device__ __forceinline__ void combination_decode(uint32_t num, uint32_t out[4]) {
+    // C(c, k) for c = 0..9, k = 4..1
+    const uint32_t c4[10] = {0, 0, 0, 0, 1, 5, 15, 35, 70, 126};
+    const uint32_t c3[10] = {0, 0, 0, 1, 4, 10, 20, 35, 56, 84};
+    const uint32_t c2[10] = {0, 0, 1, 3, 6, 10, 15, 21, 28, 36};
+    int c = 9;
+    while (c > 0 && c4[c] > num) c--;
+    num -= c4[c];
+    out[0] = c;
+    c = 9;
+    while (c > 0 && c3[c] > num) c--;
+    num -= c3[c];
+    out[1] = c;
+    c = 9;
+    while (c > 0 && c2[c] > num) c--;
+    num -= c2[c];
+    out[2] = c;
+    out[3] = num;
+}
+__host__ __device__ __forceinline__ uint32_t n_choose_4(uint32_t n) {
+    return n < 4 ? 0 : n * (n - 1) * (n - 2) * (n - 3) / 24;
+}
+
+// Order-preserving map float -> uint32 (for radix/bitonic keys).
+__device__ __forceinline__ uint32_t float_order_key(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float float_from_order_key(uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k);
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide helpers
+// ---------------------------------------------------------------------------
+
+// Ascending bitonic sort of n 64-bit keys (n arbitrary): the "flip" form of
+// the network, where every comparator points upward, so a missing partner
+// beyond n behaves as +infinity and is simply skipped.
+__device__ __forceinline__ void bitonic_sort_u64(unsigned long long* keys, uint32_t n) {
+    uint32_t npow = 1;
+    while (npow < n) npow <<= 1;
+    for (uint32_t k = 2; k <= npow; k <<= 1) {
+        // flip step
+        for (uint32_t t = threadIdx.x; t < npow / 2; t += blockDim.x) {
+            uint32_t half = k >> 1;
+            uint32_t i = (t / half) * k + (t % half);
+            uint32_t j = (t / half) * k + (k - 1 - (t % half));
+            if (j < n) {
+                unsigned long long a = keys[i], b = keys[j];
+                if (a > b) { keys[i] = b; keys[j] = a; }
+            }
+        }
+        __syncthreads();
+        for (uint32_t j = k >> 2; j > 0; j >>= 1) {
+            for (uint32_t t = threadIdx.x; t < npow / 2; t += blockDim.x) {
+                uint32_t i = (t / j) * (2 * j) + (t % j);
+                uint32_t p = i + j;
+                if (p < n) {
+                    unsigned long long a = keys[i], b = keys[p];
+                    if (a > b) { keys[i] = b; keys[p] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ uint32_t warp_sum_u32(uint32_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block reductions through a caller-provided shared array of 32 slots.
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* red) {
+    v = warp_max_u64(v);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned long long x = lane < nw ? red[lane] : 0ull;
+        x = warp_max_u64(x);
+        if (lane == 0) red[0] = x;
+    }
+    __syncthreads();
+    return red[0];
+}
+__device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t* red) {
+    v = warp_sum_u32(v);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t x = lane < nw ? red[lane] : 0u;
+        x = warp_sum_u32(x);
+        if (lane == 0) red[0] = x;
+    }
+    __syncthreads();
+    return red[0];
+}
+
+// Block exclusive scan of uint32 (returns the exclusive prefix; *total gets
+// the block total).  `red` holds 33 slots.
+__device__ __forceinline__ uint32_t block_exclusive_scan_u32(uint32_t v, uint32_t* red, uint32_t* total) {
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __syncthreads();
+    if (lane == 31) red[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t s = lane < nw ? red[lane] : 0u;
+        uint32_t t = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        red[lane] = t - s;  // exclusive prefix of warp totals
+        if (lane == 31) red[32] = t;
+    }
+    __syncthreads();
+    uint32_t r = red[wid] + x - v;
+    *total = red[32];
+    return r;
+}
+
+}  // namespace atag

@@ -1,0 +1,129 @@
+// atag_kernels.cuh — per-frame device descriptors and kernel declarations.
+#pragma once
+
+#include "atag_device.cuh"
+
+namespace atag {
+
+// Everything a kernel needs to know about one frame: its size and where its
+// buffers live in the workspace.  A batch is an array of these in device
+// memory; kernels pick their frame from blockIdx.y (pixel stages) or from a
+// flattened work index (cluster stages).
+struct FrameDesc {
+    // sizes
+    uint32_t width, height;            // after decimation
+    uint32_t factor;                   // decimation factor
+    uint32_t src_stride;               // source row pitch in bytes
+    // pixel buffers
+    const uint8_t* src;                // source frame (before decimation)
+    uint8_t* grey;                     // decimated frame (== src when factor 1)
+    uint8_t* thr;                      // thresholded
+    uint8_t* extrema;                  // optional tile min/max (2 B / tile)
+    uint8_t* filtered_extrema;         // optional dilated min/max
+    uint32_t* scratch;                 // union-find forest (w*h)
+    uint32_t* labels;                  // w*h
+    uint32_t* sizes;                   // w*h
+    atag_boundary_point* dense_points; // optional 4 planes (drop-in find_boundaries)
+    uint64_t* dense_keys;              // optional 4 planes
+    // boundary points grouped by pair (fused path)
+    unsigned long long* points;        // (pair slot << 32) | packed point
+    uint32_t point_cap;
+    // pair hash table
+    uint32_t pair_cap;                 // power of two
+    unsigned long long* pair_keys;     // EMPTY = ~0
+    uint4* pair_bbox;                  // x_min, x_max, y_min, y_max (2x coords)
+    int2* pair_gsum;                   // gx_sum, gy_sum
+    unsigned long long* pair_pxgx;     // pxgx_pygy_sum
+    uint32_t* pair_count;
+    uint32_t* pair_cluster;            // slot -> filtered cluster index or INVALID
+    // filtered clusters (sorted by pair key)
+    uint32_t cluster_cap;
+    unsigned long long* cluster_keys;
+    atag_cluster_bounds* cluster_bounds;
+    atag_cluster_extents* cluster_extents;
+    float2* cluster_center;            // (cx, cy)
+    uint32_t* cluster_cursor;
+    uint32_t* peak_count;              // per cluster
+    atag_corner* peaks;                // per cluster x 10
+    uint32_t* peak_clusters;           // rank q -> cluster
+    atag_peak_extents* peak_extents;   // rank q -> {start, count}
+    atag_fitted_quad* fitted;          // per rank q
+    atag_quad_corners* quad_tmp;       // per rank q
+    uint32_t* quad_ok;                 // per rank q
+    // cluster points
+    uint32_t cpoint_cap;
+    unsigned long long* sortbuf;       // (theta key << 32) | packed
+    atag_cluster_point* cluster_points;
+    atag_line_fit_point* line_fit;
+    float* errbuf;                     // 2 floats per point (big clusters)
+    // outputs
+    atag_quad_corners* quads;
+    uint32_t quad_cap;
+    atag_frame_stats* stats;
+    uint32_t* counters;                // per-frame work counters (see Counter)
+};
+
+// The frames a launch works on: a device table (batches) or one descriptor
+// passed by value (stage entry points, which must not allocate).  Kernels
+// receive it as a __grid_constant__ parameter, so `one` is read in place.
+struct FrameSet {
+    const FrameDesc* table;
+    FrameDesc one;
+    __device__ __forceinline__ const FrameDesc& get(uint32_t i) const { return table ? table[i] : one; }
+};
+
+// per-frame counters (FrameDesc::counters[...])
+enum Counter : uint32_t {
+    CNT_POINTS = 0,      // boundary points written
+    CNT_STATUS = 1,      // ATAG_DEVFLAG_* bits
+    CNT_CLUSTERS = 2,    // filtered clusters
+    CNT_PEAKCLU = 3,     // clusters with peaks
+    CNT_WORK = 4,        // work-queue cursor
+    CNT_COUNT = 8
+};
+
+struct PipelineParams {
+    int min_white_black_diff;
+    uint32_t min_component_size;
+    uint32_t min_cluster_pixels;
+    uint32_t tag_width;
+    int normal_border, reversed_border;
+    float max_line_fit_mse;
+    float cos_critical_f;      // float(cos(angle)) for do_indexing
+    double cos_critical_d;     // cos(angle) for the corner check
+    double min_area;           // 0.95 * min_tag_width^2
+    int compat_peak_index;
+};
+
+// k_pixels.cu
+__global__ void k_decimate(const __grid_constant__ FrameSet fs);
+__global__ void k_threshold(const __grid_constant__ FrameSet fs, int min_diff, int write_extrema);
+__global__ void k_ccl_local(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_border(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_final(const __grid_constant__ FrameSet fs);
+__global__ void k_boundaries_dense(const __grid_constant__ FrameSet fs, uint32_t min_size);
+
+// k_quads.cu (drop-in stage kernels)
+__global__ void k_fit_lines_windowed(const atag_line_fit_point* points, const uint16_t* cluster_indices,
+                                     const atag_cluster_extents* extents, size_t n, atag_corner* found);
+__global__ void k_do_indexing(const atag_peak_extents* extents, size_t count, const atag_corner* corners,
+                              const atag_line_fit_point* points, const atag_cluster_extents* cluster_extents,
+                              float max_mse, float cos_critical, atag_fitted_quad* fitted);
+__global__ void k_process_quads(const atag_fitted_quad* fitted, size_t count, PipelineParams p,
+                                atag_quad_corners* out, size_t cap, uint32_t* count_out);
+
+// k_cluster.cu (fused path)
+__global__ void k_reset_frames(const __grid_constant__ FrameSet fs);
+__global__ void k_boundaries_pairs(const __grid_constant__ FrameSet fs, uint32_t min_size);
+__global__ void k_pairs_finalize(const __grid_constant__ FrameSet fs, PipelineParams p);
+__global__ void k_scatter_points(const __grid_constant__ FrameSet fs);
+__global__ void k_cluster_fit(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets, uint32_t n_frames,
+                              uint32_t* work_counter, uint32_t sort_cap);
+__global__ void k_peaks_scan(const __grid_constant__ FrameSet fs, PipelineParams p);
+__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, uint32_t which,
+                                uint32_t* offsets, uint32_t* work_counters);
+__global__ void k_index_quads(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets, uint32_t n_frames,
+                              PipelineParams p);
+__global__ void k_compact_quads(const __grid_constant__ FrameSet fs);
+
+}  // namespace atag

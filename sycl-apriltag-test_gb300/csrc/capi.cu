@@ -1,0 +1,645 @@
+// capi.cu — the C ABI (include/atag.h): argument checking, workspace
+// layout, and the stream-ordered launch sequence of the detector.
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "atag_kernels.cuh"
+
+using namespace atag;
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
+
+atag_status fail(atag_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return s;
+}
+
+#define CK(call)                                                                                    \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) return fail(ATAG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define LAUNCHED()                                                                                  \
+    do {                                                                                            \
+        g_launches.fetch_add(1, std::memory_order_relaxed);                                         \
+        cudaError_t e_ = cudaGetLastError();                                                        \
+        if (e_ != cudaSuccess) return fail(ATAG_ERR_CUDA, "launch: %s", cudaGetErrorString(e_));   \
+    } while (0)
+
+struct DeviceInfo {
+    int device = -1;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+};
+
+std::mutex g_init_mutex;
+DeviceInfo g_dev[64];
+
+constexpr uint32_t SORT_CAP = 12288;  // cluster points sorted in shared memory (96 KB)
+
+atag_status ensure_device(DeviceInfo** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(ATAG_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= 64) return fail(ATAG_ERR_NO_DEVICE, "device ordinal %d unsupported", dev);
+    std::lock_guard<std::mutex> lk(g_init_mutex);
+    DeviceInfo& d = g_dev[dev];
+    if (d.device != dev) {
+        cudaDeviceProp prop;
+        CK(cudaGetDeviceProperties(&prop, dev));
+        if (!(prop.major == 10 && prop.minor == 3))
+            return fail(ATAG_ERR_NO_DEVICE, "device %d is sm_%d%d; this library is built for sm_103a only", dev,
+                        prop.major, prop.minor);
+        cudaFuncAttributes fa;
+        e = cudaFuncGetAttributes(&fa, k_threshold);
+        if (e != cudaSuccess) return fail(ATAG_ERR_NO_DEVICE, "kernels do not load: %s", cudaGetErrorString(e));
+        CK(cudaFuncSetAttribute(k_cluster_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(SORT_CAP * sizeof(unsigned long long))));
+        d.num_sms = prop.multiProcessorCount;
+        d.smem_optin = prop.sharedMemPerBlockOptin;
+        d.device = dev;
+    }
+    *out = &d;
+    return ATAG_OK;
+}
+
+bool valid_dims(size_t w, size_t h) { return w >= 4 && h >= 4 && w % 4 == 0 && h % 4 == 0 && w <= 4096 && h <= 4096; }
+
+PipelineParams make_params(const atag_config& c) {
+    PipelineParams p;
+    p.min_white_black_diff = c.min_white_black_diff;
+    p.min_component_size = (uint32_t)c.min_component_size;
+    p.min_cluster_pixels = (uint32_t)c.min_cluster_pixels;
+    p.tag_width = (uint32_t)c.tag_width;
+    p.normal_border = c.normal_border;
+    p.reversed_border = c.reversed_border;
+    p.max_line_fit_mse = c.max_line_fit_mse;
+    double cr = std::cos((double)c.critical_angle_deg * M_PI / 180);
+    p.cos_critical_f = (float)cr;
+    p.cos_critical_d = cr;
+    p.min_area = 0.95 * c.min_tag_width * c.min_tag_width;
+    p.compat_peak_index = c.compat_peak_index;
+    return p;
+}
+
+dim3 grid2(size_t x, size_t y) {
+    if (x < 1) x = 1;
+    if (x > 65535u * 32) x = 65535u * 32;
+    return dim3((unsigned)x, (unsigned)y);
+}
+size_t cdiv(size_t a, size_t b) { return (a + b - 1) / b; }
+
+FrameSet single(const FrameDesc& d) {
+    FrameSet s;
+    memset(&s, 0, sizeof s);
+    s.table = nullptr;
+    s.one = d;
+    return s;
+}
+FrameDesc blank() {
+    FrameDesc d;
+    memset(&d, 0, sizeof d);
+    return d;
+}
+
+// -------------------------------------------------------------------------
+// workspace layout
+// -------------------------------------------------------------------------
+constexpr size_t ALIGN = 256;
+size_t al(size_t v) { return (v + ALIGN - 1) / ALIGN * ALIGN; }
+uint32_t pow2_at_least(uint32_t v) {
+    uint32_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+struct FrameCaps {
+    uint32_t point_cap, pair_cap, cluster_cap, cpoint_cap;
+};
+FrameCaps caps_for(size_t N) {
+    FrameCaps c;
+    c.point_cap = (uint32_t)std::max<size_t>(2 * N, 4096);
+    size_t pc = std::min<size_t>(std::max<size_t>(N / 512, 1024), 65536);
+    c.pair_cap = pow2_at_least((uint32_t)pc);
+    c.cluster_cap = (uint32_t)std::min<size_t>(std::max<size_t>(N / 1024, 512), 65535);
+    c.cpoint_cap = (uint32_t)std::max<size_t>(N / 2, 4096);
+    return c;
+}
+
+// Lays out one frame's buffers at `base` (device address, may be 0 to only
+// measure).  Returns the bytes used.
+size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, FrameDesc* d) {
+    size_t N = (size_t)w * h;
+    FrameCaps c = caps_for(N);
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char* {
+        char* p = base ? base + off : nullptr;
+        off += al(bytes);
+        return p;
+    };
+    FrameDesc f = blank();
+    f.width = w;
+    f.height = h;
+    f.factor = factor;
+    f.grey = factor > 1 ? (uint8_t*)take(N) : nullptr;
+    f.thr = (uint8_t*)take(N);
+    f.scratch = (uint32_t*)take(4 * N);
+    f.labels = (uint32_t*)take(4 * N);
+    f.sizes = (uint32_t*)take(4 * N);
+    f.point_cap = c.point_cap;
+    f.points = (unsigned long long*)take(8ull * c.point_cap);
+    f.pair_cap = c.pair_cap;
+    f.pair_keys = (unsigned long long*)take(8ull * c.pair_cap);
+    f.pair_bbox = (uint4*)take(16ull * c.pair_cap);
+    f.pair_gsum = (int2*)take(8ull * c.pair_cap);
+    f.pair_pxgx = (unsigned long long*)take(8ull * c.pair_cap);
+    f.pair_count = (uint32_t*)take(4ull * c.pair_cap);
+    f.pair_cluster = (uint32_t*)take(4ull * c.pair_cap);
+    f.cluster_cap = c.cluster_cap;
+    f.cluster_keys = (unsigned long long*)take(8ull * ((size_t)c.cluster_cap + c.pair_cap));
+    f.cluster_bounds = (atag_cluster_bounds*)take(sizeof(atag_cluster_bounds) * c.cluster_cap);
+    f.cluster_extents = (atag_cluster_extents*)take(sizeof(atag_cluster_extents) * c.cluster_cap);
+    f.cluster_center = (float2*)take(8ull * c.cluster_cap);
+    f.cluster_cursor = (uint32_t*)take(4ull * c.cluster_cap);
+    f.peak_count = (uint32_t*)take(4ull * c.cluster_cap);
+    f.peaks = (atag_corner*)take(sizeof(atag_corner) * 10ull * c.cluster_cap);
+    f.peak_clusters = (uint32_t*)take(4ull * c.cluster_cap);
+    f.peak_extents = (atag_peak_extents*)take(sizeof(atag_peak_extents) * c.cluster_cap);
+    f.fitted = (atag_fitted_quad*)take(sizeof(atag_fitted_quad) * c.cluster_cap);
+    f.quad_tmp = (atag_quad_corners*)take(sizeof(atag_quad_corners) * c.cluster_cap);
+    f.quad_ok = (uint32_t*)take(4ull * c.cluster_cap);
+    f.cpoint_cap = c.cpoint_cap;
+    f.sortbuf = (unsigned long long*)take(8ull * c.cpoint_cap);
+    f.cluster_points = (atag_cluster_point*)take(sizeof(atag_cluster_point) * c.cpoint_cap);
+    f.line_fit = (atag_line_fit_point*)take(sizeof(atag_line_fit_point) * c.cpoint_cap);
+    f.errbuf = (float*)take(8ull * c.cpoint_cap);
+    f.counters = (uint32_t*)take(4ull * CNT_COUNT);
+    if (d) *d = f;
+    return off;
+}
+
+constexpr int RING = 16;
+
+}  // namespace
+
+// ===========================================================================
+// detector
+// ===========================================================================
+struct atag_detector {
+    atag_config cfg;
+    PipelineParams pp;
+    size_t max_w, max_h, max_frames, max_total_pixels;
+    DeviceInfo* dev = nullptr;
+    char* ws = nullptr;
+    size_t ws_bytes = 0;
+    bool owns_ws = false;
+    // header carve-out
+    FrameDesc* d_tables = nullptr;   // RING x max_frames
+    uint32_t* d_work = nullptr;      // offsets (2 x (max_frames + 1)) + 2 counters
+    uint8_t* d_input = nullptr;      // host-upload input region
+    size_t input_bytes = 0;
+    atag_quad_corners* d_hquads = nullptr;  // host-path quad staging
+    atag_frame_stats* d_hstats = nullptr;
+    size_t hquad_cap = 0;
+    char* frames_base = nullptr;
+    size_t frames_bytes = 0;
+    // host staging for the frame tables
+    FrameDesc* h_staging = nullptr;  // pinned, RING x max_frames
+    cudaEvent_t ev[RING];
+    int ring = 0;
+    int last_slot = -1;
+    std::vector<FrameDesc> last;     // table last uploaded
+    std::vector<FrameDesc> cur;      // table of the last call
+};
+
+namespace {
+
+constexpr size_t HOST_QUAD_CAP = 4096;
+
+size_t header_bytes(size_t max_frames, size_t input_bytes) {
+    size_t b = 0;
+    b += al(sizeof(FrameDesc) * RING * max_frames);
+    b += al(4 * (2 * (max_frames + 1) + 2));
+    b += al(input_bytes);
+    b += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
+    b += al(sizeof(atag_frame_stats));
+    return b;
+}
+
+size_t frames_bound(size_t max_frames, size_t max_total_pixels) {
+    // bytes(N) is bounded by a per-frame constant plus a per-pixel slope
+    size_t c0 = layout_frame(nullptr, 4, 4, 2, nullptr);
+    size_t big = 1 << 22;  // 4 Mpx
+    size_t cb = layout_frame(nullptr, 2048, 2048, 2, nullptr);
+    double slope = (double)(cb) / (double)big;
+    return max_frames * (c0 + 64 * ALIGN) + (size_t)(slope * 1.25 * (double)max_total_pixels) + (1 << 20);
+}
+
+}  // namespace
+
+extern "C" {
+
+void atag_config_default(atag_config* c) {
+    c->decimate = 1;
+    c->min_white_black_diff = 5;
+    c->min_component_size = 25;
+    c->min_cluster_pixels = 5;
+    c->tag_width = 4;
+    c->normal_border = 1;
+    c->reversed_border = 0;
+    c->max_line_fit_mse = 10.0f;
+    c->critical_angle_deg = 10.0f;
+    c->min_tag_width = 8;
+    c->compat_peak_index = 1;
+}
+
+const char* atag_status_string(atag_status s) {
+    switch (s) {
+    case ATAG_OK: return "ok";
+    case ATAG_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case ATAG_ERR_CUDA: return "CUDA error";
+    case ATAG_ERR_CAPACITY: return "capacity exceeded";
+    case ATAG_ERR_ITERATION_CAP: return "iteration cap reached";
+    case ATAG_ERR_NO_DEVICE: return "no suitable device";
+    case ATAG_ERR_OUT_OF_MEMORY: return "out of memory";
+    }
+    return "unknown status";
+}
+
+const char* atag_last_error(void) { return g_last_error.c_str(); }
+
+atag_status atag_init(void) {
+    DeviceInfo* d;
+    return ensure_device(&d);
+}
+
+uint64_t atag_launch_count(void) { return g_launches.load(); }
+
+// ------------------------------------------------------------------ stages
+
+atag_status atag_decimate(const uint8_t* src, size_t sw, size_t sh, size_t f, uint8_t* dst, atag_stream_t stream) {
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    if (!src || !dst || f < 1 || f > 64) return fail(ATAG_ERR_INVALID_ARGUMENT, "decimate: bad pointer or factor");
+    size_t w = sw / f, h = sh / f;
+    if (!valid_dims(w, h)) return fail(ATAG_ERR_INVALID_ARGUMENT, "decimate: %zux%zu after decimation is not a multiple of 4 in [4, 4096]", w, h);
+    if (f == 1) {
+        CK(cudaMemcpyAsync(dst, src, sw * sh, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+        return ATAG_OK;
+    }
+    FrameDesc d = blank();
+    d.width = (uint32_t)w; d.height = (uint32_t)h; d.factor = (uint32_t)f; d.src_stride = (uint32_t)sw;
+    d.src = src; d.grey = dst;
+    k_decimate<<<grid2(std::min<size_t>(cdiv(w / 4 * h, 256), 4096), 1), 256, 0, (cudaStream_t)stream>>>(single(d));
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+atag_status atag_threshold_image(const uint8_t* grey, uint8_t* extrema, uint8_t* filtered, uint8_t* thr,
+                                 size_t w, size_t h, atag_stream_t stream) {
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    if (!grey || !thr) return fail(ATAG_ERR_INVALID_ARGUMENT, "threshold_image: null pointer");
+    if (!valid_dims(w, h)) return fail(ATAG_ERR_INVALID_ARGUMENT, "threshold_image: %zux%zu is not a multiple of 4 in [4, 4096]", w, h);
+    FrameDesc d = blank();
+    d.width = (uint32_t)w; d.height = (uint32_t)h; d.factor = 1;
+    d.grey = const_cast<uint8_t*>(grey); d.thr = thr; d.extrema = extrema; d.filtered_extrema = filtered;
+    size_t tiles = cdiv(w / 4, 32) * cdiv(h / 4, 8);
+    k_threshold<<<grid2(tiles, 1), 256, 0, (cudaStream_t)stream>>>(single(d), 5, (extrema || filtered) ? 1 : 0);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+static atag_status launch_segmentation(const FrameSet& fs, size_t max_w, size_t max_h, size_t nf, cudaStream_t s) {
+    size_t tiles = cdiv(max_w / 2, 32) * cdiv(max_h / 2, 16);
+    k_ccl_local<<<grid2(tiles, nf), 512, 0, s>>>(fs);
+    LAUNCHED();
+    size_t border = tiles * (32 + 2 * (16 - 1));
+    k_ccl_border<<<grid2(cdiv(border, 256), nf), 256, 0, s>>>(fs);
+    LAUNCHED();
+    size_t blocks = (max_w / 2) * (max_h / 2);
+    k_ccl_final<<<grid2(std::min<size_t>(cdiv(blocks, 256), 8192), nf), 256, 0, s>>>(fs);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+atag_status atag_image_segmentation(const uint8_t* thr, uint32_t* scratch, uint32_t* labels, uint32_t* sizes,
+                                    size_t sizes_elem, size_t w, size_t h, atag_stream_t stream) {
+    (void)sizes_elem;
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    if (!thr || !scratch || !labels || !sizes) return fail(ATAG_ERR_INVALID_ARGUMENT, "image_segmentation: null pointer");
+    if (!valid_dims(w, h)) return fail(ATAG_ERR_INVALID_ARGUMENT, "image_segmentation: %zux%zu is not a multiple of 4 in [4, 4096]", w, h);
+    FrameDesc d = blank();
+    d.width = (uint32_t)w; d.height = (uint32_t)h; d.factor = 1;
+    d.thr = const_cast<uint8_t*>(thr); d.scratch = scratch; d.labels = labels; d.sizes = sizes;
+    return launch_segmentation(single(d), w, h, 1, (cudaStream_t)stream);
+}
+
+atag_status atag_find_boundaries(const uint32_t* labels, const uint32_t* sizes, atag_boundary_point* points,
+                                 uint64_t* blob_labels, size_t w, size_t h, atag_stream_t stream) {
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    if (!labels || !sizes || !points || !blob_labels) return fail(ATAG_ERR_INVALID_ARGUMENT, "find_boundaries: null pointer");
+    if (!valid_dims(w, h)) return fail(ATAG_ERR_INVALID_ARGUMENT, "find_boundaries: %zux%zu is not a multiple of 4 in [4, 4096]", w, h);
+    FrameDesc d = blank();
+    d.width = (uint32_t)w; d.height = (uint32_t)h;
+    d.labels = const_cast<uint32_t*>(labels); d.sizes = const_cast<uint32_t*>(sizes);
+    d.dense_points = points; d.dense_keys = blob_labels;
+    k_boundaries_dense<<<grid2(std::min<size_t>(cdiv(w * h, 256), 8192), 1), 256, 0, (cudaStream_t)stream>>>(single(d), 25);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+atag_status atag_fit_lines(const atag_line_fit_point* points, const uint16_t* cidx, const atag_cluster_extents* extents,
+                           size_t n, atag_corner* found, atag_stream_t stream) {
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    if (n == 0) return ATAG_OK;
+    if (!points || !cidx || !extents || !found) return fail(ATAG_ERR_INVALID_ARGUMENT, "fit_lines: null pointer");
+    size_t groups = cdiv(n, 24);
+    k_fit_lines_windowed<<<grid2(cdiv(groups, 4), 1), 128, 0, (cudaStream_t)stream>>>(points, cidx, extents, n, found);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+atag_status atag_do_indexing(const atag_peak_extents* extents, size_t count, const atag_corner* corners,
+                             const atag_line_fit_point* points, const atag_cluster_extents* cluster_extents,
+                             atag_fitted_quad* fitted, atag_stream_t stream) {
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    if (count == 0) return ATAG_OK;
+    if (!extents || !corners || !points || !cluster_extents || !fitted)
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "do_indexing: null pointer");
+    float cosc = (float)std::cos(10 * M_PI / 180);
+    k_do_indexing<<<grid2(std::min<size_t>(count, 65535), 1), 256, 0, (cudaStream_t)stream>>>(
+        extents, count, corners, points, cluster_extents, 10.0f, cosc, fitted);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+atag_status atag_process_fitted_quads(const atag_fitted_quad* fitted, size_t count, size_t w, size_t h,
+                                      const atag_config* cfg, atag_quad_corners* quads, size_t cap, uint32_t* d_count,
+                                      atag_stream_t stream) {
+    (void)w; (void)h;
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    if (!d_count || (count && (!fitted || !quads))) return fail(ATAG_ERR_INVALID_ARGUMENT, "process_fitted_quads: null pointer");
+    atag_config c;
+    if (cfg) c = *cfg; else atag_config_default(&c);
+    k_process_quads<<<1, 256, 0, (cudaStream_t)stream>>>(fitted, count, make_params(c), quads, cap, d_count);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+// ------------------------------------------------------------------ detector
+
+atag_status atag_workspace_size(const atag_config* cfg, size_t max_w, size_t max_h, size_t max_frames,
+                                size_t max_total_pixels, size_t* bytes) {
+    if (!bytes || max_frames == 0) return fail(ATAG_ERR_INVALID_ARGUMENT, "workspace_size: bad argument");
+    atag_config c;
+    if (cfg) c = *cfg; else atag_config_default(&c);
+    if (c.decimate < 1) return fail(ATAG_ERR_INVALID_ARGUMENT, "workspace_size: decimate < 1");
+    if (!valid_dims(max_w, max_h)) return fail(ATAG_ERR_INVALID_ARGUMENT, "workspace_size: bad max dimensions");
+    if (max_total_pixels == 0) max_total_pixels = max_w * max_h * max_frames;
+    size_t input = max_total_pixels * (size_t)c.decimate * (size_t)c.decimate;
+    *bytes = header_bytes(max_frames, input) + frames_bound(max_frames, max_total_pixels);
+    return ATAG_OK;
+}
+
+atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t max_h, size_t max_frames,
+                                 size_t max_total_pixels, void* d_ws, size_t ws_bytes, atag_detector** out) {
+    if (!out) return fail(ATAG_ERR_INVALID_ARGUMENT, "detector_create: null out");
+    *out = nullptr;
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    atag_config c;
+    if (cfg) c = *cfg; else atag_config_default(&c);
+    if (max_total_pixels == 0) max_total_pixels = max_w * max_h * max_frames;
+    size_t need;
+    st = atag_workspace_size(&c, max_w, max_h, max_frames, max_total_pixels, &need);
+    if (st) return st;
+    if (d_ws && ws_bytes < need) return fail(ATAG_ERR_OUT_OF_MEMORY, "detector_create: workspace of %zu bytes < %zu needed", ws_bytes, need);
+    atag_detector* det = new atag_detector();
+    det->cfg = c;
+    det->pp = make_params(c);
+    det->max_w = max_w; det->max_h = max_h; det->max_frames = max_frames; det->max_total_pixels = max_total_pixels;
+    det->dev = dev;
+    if (d_ws) {
+        det->ws = (char*)d_ws;
+        det->ws_bytes = ws_bytes;
+    } else {
+        cudaError_t e = cudaMalloc(&det->ws, need);
+        if (e != cudaSuccess) {
+            delete det;
+            return fail(ATAG_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu): %s", need, cudaGetErrorString(e));
+        }
+        det->ws_bytes = need;
+        det->owns_ws = true;
+    }
+    char* p = det->ws;
+    det->d_tables = (FrameDesc*)p; p += al(sizeof(FrameDesc) * RING * max_frames);
+    det->d_work = (uint32_t*)p; p += al(4 * (2 * (max_frames + 1) + 2));
+    det->input_bytes = max_total_pixels * (size_t)c.decimate * (size_t)c.decimate;
+    det->d_input = (uint8_t*)p; p += al(det->input_bytes);
+    det->d_hquads = (atag_quad_corners*)p; p += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
+    det->d_hstats = (atag_frame_stats*)p; p += al(sizeof(atag_frame_stats));
+    det->hquad_cap = HOST_QUAD_CAP;
+    det->frames_base = p;
+    det->frames_bytes = det->ws_bytes - (size_t)(p - det->ws);
+    cudaError_t e = cudaHostAlloc(&det->h_staging, sizeof(FrameDesc) * RING * max_frames, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        if (det->owns_ws) cudaFree(det->ws);
+        delete det;
+        return fail(ATAG_ERR_OUT_OF_MEMORY, "cudaHostAlloc: %s", cudaGetErrorString(e));
+    }
+    for (int i = 0; i < RING; i++) cudaEventCreateWithFlags(&det->ev[i], cudaEventDisableTiming);
+    *out = det;
+    return ATAG_OK;
+}
+
+atag_status atag_detector_destroy(atag_detector* det) {
+    if (!det) return ATAG_OK;
+    for (int i = 0; i < RING; i++) {
+        cudaEventSynchronize(det->ev[i]);
+        cudaEventDestroy(det->ev[i]);
+    }
+    if (det->h_staging) cudaFreeHost(det->h_staging);
+    if (det->owns_ws) cudaFree(det->ws);
+    delete det;
+    return ATAG_OK;
+}
+
+static atag_status upload_table(atag_detector* det, const std::vector<FrameDesc>& t, cudaStream_t s,
+                                const FrameDesc** d_table) {
+    size_t n = t.size();
+    if (det->last_slot >= 0 && det->last.size() == n && memcmp(det->last.data(), t.data(), n * sizeof(FrameDesc)) == 0) {
+        *d_table = det->d_tables + (size_t)det->last_slot * det->max_frames;
+        return ATAG_OK;
+    }
+    int slot = det->ring;
+    det->ring = (det->ring + 1) % RING;
+    CK(cudaEventSynchronize(det->ev[slot]));  // the slot's previous upload has been consumed by its copy
+    FrameDesc* h = det->h_staging + (size_t)slot * det->max_frames;
+    memcpy(h, t.data(), n * sizeof(FrameDesc));
+    FrameDesc* d = det->d_tables + (size_t)slot * det->max_frames;
+    CK(cudaMemcpyAsync(d, h, n * sizeof(FrameDesc), cudaMemcpyHostToDevice, s));
+    CK(cudaEventRecord(det->ev[slot], s));
+    det->last = t;
+    det->last_slot = slot;
+    *d_table = d;
+    return ATAG_OK;
+}
+
+atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size_t n, atag_quad_corners* d_quads,
+                              size_t quad_cap, atag_frame_stats* d_stats, atag_stream_t stream) {
+    if (!det || !frames || n == 0 || !d_quads || !d_stats) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: bad argument");
+    if (n > det->max_frames) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: %zu frames > max %zu", n, det->max_frames);
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t f = (uint32_t)det->cfg.decimate;
+    std::vector<FrameDesc> t(n);
+    size_t off = 0, total_px = 0, mw = 0, mh = 0, max_pair = 0, max_points = 0;
+    bool any_decim = f > 1;
+    for (size_t i = 0; i < n; i++) {
+        const atag_frame& fr = frames[i];
+        if (!fr.d_grey) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu has no image", i);
+        size_t w = fr.src_width / f, h = fr.src_height / f;
+        if (!valid_dims(w, h) || w > det->max_w || h > det->max_h)
+            return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu is %ux%u; after decimation by %u it must be a multiple of 4 within %zux%zu",
+                        i, fr.src_width, fr.src_height, f, det->max_w, det->max_h);
+        total_px += w * h;
+        if (total_px > det->max_total_pixels) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: batch exceeds %zu pixels", det->max_total_pixels);
+        size_t bytes = layout_frame(det->frames_base + off, (uint32_t)w, (uint32_t)h, f, &t[i]);
+        off += bytes;
+        if (off > det->frames_bytes) return fail(ATAG_ERR_OUT_OF_MEMORY, "detect_batch: workspace too small");
+        FrameDesc& d = t[i];
+        d.src = fr.d_grey;
+        d.src_stride = fr.src_width;
+        if (f == 1) d.grey = const_cast<uint8_t*>(fr.d_grey);
+        d.quads = d_quads + i * quad_cap;
+        d.quad_cap = (uint32_t)quad_cap;
+        d.stats = d_stats + i;
+        mw = std::max(mw, w); mh = std::max(mh, h);
+        max_pair = std::max<size_t>(max_pair, d.pair_cap);
+        max_points = std::max<size_t>(max_points, d.point_cap);
+    }
+    const FrameDesc* d_table;
+    atag_status st = upload_table(det, t, s, &d_table);
+    if (st) return st;
+    det->cur = t;
+    FrameSet fs;
+    memset(&fs, 0, sizeof fs);
+    fs.table = d_table;
+    const PipelineParams& p = det->pp;
+    const int sms = det->dev->num_sms;
+    uint32_t* off_clusters = det->d_work;
+    uint32_t* off_peaks = det->d_work + (n + 1);
+    uint32_t* wc = det->d_work + 2 * (det->max_frames + 1);
+
+    k_reset_frames<<<grid2(cdiv(max_pair, 256), n), 256, 0, s>>>(fs);
+    LAUNCHED();
+    if (any_decim) {
+        k_decimate<<<grid2(std::min<size_t>(cdiv(mw / 4 * mh, 256), 2048), n), 256, 0, s>>>(fs);
+        LAUNCHED();
+    }
+    k_threshold<<<grid2(cdiv(mw / 4, 32) * cdiv(mh / 4, 8), n), 256, 0, s>>>(fs, p.min_white_black_diff, 0);
+    LAUNCHED();
+    st = launch_segmentation(fs, mw, mh, n, s);
+    if (st) return st;
+    k_boundaries_pairs<<<grid2(cdiv(mw, 64) * cdiv(mh, 16), n), 256, 0, s>>>(fs, p.min_component_size);
+    LAUNCHED();
+    k_pairs_finalize<<<(unsigned)n, 1024, 0, s>>>(fs, p);
+    LAUNCHED();
+    k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_CLUSTERS, off_clusters, wc);
+    LAUNCHED();
+    k_scatter_points<<<grid2(std::min<size_t>(cdiv(max_points, 256), 1024), n), 256, 0, s>>>(fs);
+    LAUNCHED();
+    k_cluster_fit<<<sms, 512, SORT_CAP * sizeof(unsigned long long), s>>>(fs, off_clusters, (uint32_t)n, wc, SORT_CAP);
+    LAUNCHED();
+    k_peaks_scan<<<(unsigned)n, 1024, 0, s>>>(fs, p);
+    LAUNCHED();
+    k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_PEAKCLU, off_peaks, wc + 1);
+    LAUNCHED();
+    k_index_quads<<<sms * 8, 256, 0, s>>>(fs, off_peaks, (uint32_t)n, p);
+    LAUNCHED();
+    k_compact_quads<<<(unsigned)n, 1024, 0, s>>>(fs);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+atag_status atag_detect(atag_detector* det, const uint8_t* d_grey, size_t sw, size_t sh, atag_quad_corners* d_quads,
+                        size_t quad_cap, atag_frame_stats* d_stats, atag_stream_t stream) {
+    atag_frame fr{d_grey, (uint32_t)sw, (uint32_t)sh};
+    return atag_detect_batch(det, &fr, 1, d_quads, quad_cap, d_stats, stream);
+}
+
+atag_status atag_detect_host(atag_detector* det, const uint8_t* h_grey, size_t sw, size_t sh, atag_quad_corners* h_quads,
+                             size_t quad_cap, atag_frame_stats* h_stats, atag_stream_t stream) {
+    if (!det || !h_grey || !h_stats || (quad_cap && !h_quads)) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_host: bad argument");
+    if (sw * sh > det->input_bytes) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_host: frame larger than the detector's input region");
+    cudaStream_t s = (cudaStream_t)stream;
+    size_t cap = std::min(quad_cap, det->hquad_cap);
+    CK(cudaMemcpyAsync(det->d_input, h_grey, sw * sh, cudaMemcpyHostToDevice, s));
+    atag_status st = atag_detect(det, det->d_input, sw, sh, det->d_hquads, det->hquad_cap, det->d_hstats, stream);
+    if (st) return st;
+    CK(cudaMemcpyAsync(h_stats, det->d_hstats, sizeof(atag_frame_stats), cudaMemcpyDeviceToHost, s));
+    if (cap) CK(cudaMemcpyAsync(h_quads, det->d_hquads, sizeof(atag_quad_corners) * cap, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return ATAG_OK;
+}
+
+atag_status atag_detector_views(const atag_detector* det, size_t frame, atag_frame_views* out) {
+    if (!det || !out || frame >= det->cur.size()) return fail(ATAG_ERR_INVALID_ARGUMENT, "detector_views: bad frame");
+    const FrameDesc& d = det->cur[frame];
+    memset(out, 0, sizeof *out);
+    out->decimated = d.grey;
+    out->thresholded = d.thr;
+    out->labels = d.labels;
+    out->sizes = d.sizes;
+    out->pair_points = (const uint64_t*)d.points;
+    out->pair_keys = (const uint64_t*)d.pair_keys;
+    out->pair_capacity = d.pair_cap;
+    out->cluster_keys = (const uint64_t*)d.cluster_keys;
+    out->cluster_bounds = d.cluster_bounds;
+    out->cluster_extents = d.cluster_extents;
+    out->cluster_points = d.cluster_points;
+    out->line_fit_points = d.line_fit;
+    out->peak_count = d.peak_count;
+    out->peaks = d.peaks;
+    out->peak_clusters = d.peak_clusters;
+    out->peak_extents = d.peak_extents;
+    out->fitted = d.fitted;
+    return ATAG_OK;
+}
+
+atag_status atag_use_device(int ordinal) {
+    cudaError_t e = cudaSetDevice(ordinal);
+    if (e != cudaSuccess) return fail(ATAG_ERR_NO_DEVICE, "cudaSetDevice(%d): %s", ordinal, cudaGetErrorString(e));
+    DeviceInfo* d;
+    return ensure_device(&d);
+}
+
+}  // extern "C"

@@ -1,0 +1,704 @@
+// k_cluster.cu — the fused path from labels to quads.
+//
+// The reference groups boundary points with a global 64-bit sort_by_key over
+// every point (main.cpp:515), reduces ClusterBounds per key (:571-585),
+// filters, maps points back to clusters with a binary search (:621-675) and
+// sorts again by (cluster, theta) (:737).  Only the ORDER of the surviving
+// clusters and the ORDER of points inside a cluster influence the result,
+// and both are fixed by keys, so here:
+//   1. k_boundaries_pairs: each CTA finds its boundary points, aggregates
+//      them per cluster pair in a shared-memory hash table (warp-level
+//      reductions first), merges the per-pair ClusterBounds sums into a
+//      per-frame global hash table with one set of atomics per (CTA, pair),
+//      and appends its points, tagged with their pair slot, to a list;
+//   2. k_pairs_finalize: one CTA per frame sorts the distinct pair keys
+//      (hundreds to a few thousand), applies ValidBlobFilter and assigns
+//      each surviving pair its cluster index and extent;
+//   3. k_scatter_points: points of surviving pairs go straight into their
+//      cluster's segment with their theta key; the rest are dropped;
+//   4. k_cluster_fit: one CTA per cluster sorts by (theta, point) in shared
+//      memory and does line-fit moments, the prefix scan, the windowed
+//      errors, the 7-tap filter and the peak search (fit_lines), keeping
+//      the 10 best peaks;
+//   5. k_peaks_scan / k_index_quads / k_compact_quads: peak extents,
+//      do_indexing and the corner intersection, quads in reference order.
+#include "atag_kernels.cuh"
+#include "atag_quads.cuh"
+
+namespace atag {
+
+constexpr unsigned long long EMPTY_KEY = ~0ull;
+
+__device__ __forceinline__ uint32_t hash_key(unsigned long long k) {
+    return (uint32_t)((k * 0x9E3779B97F4A7C15ull) >> 32);
+}
+
+// ---------------------------------------------------------------------------
+// reset
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_reset_frames(const __grid_constant__ FrameSet fs) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < F.pair_cap; i += gridDim.x * blockDim.x) {
+        F.pair_keys[i] = EMPTY_KEY;
+        F.pair_bbox[i] = make_uint4(0xFFFFFFFFu, 0u, 0xFFFFFFFFu, 0u);
+        F.pair_gsum[i] = make_int2(0, 0);
+        F.pair_pxgx[i] = 0ull;
+        F.pair_count[i] = 0u;
+        F.pair_cluster[i] = INVALID;
+    }
+    if (blockIdx.x == 0 && threadIdx.x < CNT_COUNT) F.counters[threadIdx.x] = 0u;
+}
+
+// ---------------------------------------------------------------------------
+// 1. boundaries + per-pair aggregation
+// ---------------------------------------------------------------------------
+constexpr int BP_W = 64, BP_H = 16;            // pixels per CTA tile
+constexpr int BP_SW = BP_W + 2, BP_SH = BP_H + 1;
+constexpr int BP_LC = 256;                     // CTA hash-table entries
+constexpr int BP_THREADS = 256;                // 4 pixels per thread
+
+struct Agg {
+    unsigned long long key;
+    uint32_t cnt, xmin, xmax, ymin, ymax;
+    int gx, gy, pxgx;
+};
+
+__device__ __forceinline__ void agg_init(Agg& a, unsigned long long key) {
+    a.key = key;
+    a.cnt = 0; a.xmin = 0xFFFFFFFFu; a.xmax = 0; a.ymin = 0xFFFFFFFFu; a.ymax = 0;
+    a.gx = 0; a.gy = 0; a.pxgx = 0;
+}
+__device__ __forceinline__ void agg_add(Agg& a, uint32_t packed) {
+    uint32_t xd = bp_xd(packed), yd = bp_yd(packed);
+    int gx = bp_gx(packed), gy = bp_gy(packed);
+    a.cnt += 1;
+    a.xmin = min(a.xmin, xd); a.xmax = max(a.xmax, xd);
+    a.ymin = min(a.ymin, yd); a.ymax = max(a.ymax, yd);
+    a.gx += gx; a.gy += gy;
+    a.pxgx += (int)xd * gx + (int)yd * gy;
+}
+
+struct PairTableSmem {
+    unsigned long long key[BP_LC];
+    uint32_t cnt[BP_LC], xmin[BP_LC], xmax[BP_LC], ymin[BP_LC], ymax[BP_LC];
+    int gx[BP_LC], gy[BP_LC];
+    unsigned long long pxgx[BP_LC];
+    uint32_t gslot[BP_LC];
+};
+
+__device__ __forceinline__ int local_insert(PairTableSmem& T, unsigned long long key) {
+    uint32_t h = hash_key(key) & (BP_LC - 1);
+    for (int p = 0; p < BP_LC; p++) {
+        unsigned long long k = atomicCAS(&T.key[h], EMPTY_KEY, key);
+        if (k == EMPTY_KEY || k == key) return (int)h;
+        h = (h + 1) & (BP_LC - 1);
+    }
+    return -1;
+}
+__device__ __forceinline__ int local_lookup(const PairTableSmem& T, unsigned long long key) {
+    uint32_t h = hash_key(key) & (BP_LC - 1);
+    for (int p = 0; p < BP_LC; p++) {
+        unsigned long long k = T.key[h];
+        if (k == key) return (int)h;
+        if (k == EMPTY_KEY) return -1;
+        h = (h + 1) & (BP_LC - 1);
+    }
+    return -1;
+}
+__device__ __forceinline__ uint32_t global_insert(const FrameDesc& F, unsigned long long key) {
+    uint32_t mask = F.pair_cap - 1, h = hash_key(key) & mask;
+    for (uint32_t p = 0; p < F.pair_cap; p++) {
+        unsigned long long k = atomicCAS(&F.pair_keys[h], EMPTY_KEY, key);
+        if (k == EMPTY_KEY || k == key) return h;
+        h = (h + 1) & mask;
+    }
+    return INVALID;
+}
+__device__ __forceinline__ uint32_t global_lookup(const FrameDesc& F, unsigned long long key) {
+    uint32_t mask = F.pair_cap - 1, h = hash_key(key) & mask;
+    for (uint32_t p = 0; p < F.pair_cap; p++) {
+        unsigned long long k = F.pair_keys[h];
+        if (k == key) return h;
+        if (k == EMPTY_KEY) return INVALID;
+        h = (h + 1) & mask;
+    }
+    return INVALID;
+}
+__device__ __forceinline__ void global_flush(const FrameDesc& F, uint32_t gs, uint32_t cnt, uint32_t xmin,
+                                             uint32_t xmax, uint32_t ymin, uint32_t ymax, int gx, int gy,
+                                             unsigned long long pxgx) {
+    atomicAdd(&F.pair_count[gs], cnt);
+    uint32_t* bb = reinterpret_cast<uint32_t*>(&F.pair_bbox[gs]);
+    atomicMin(bb + 0, xmin);
+    atomicMax(bb + 1, xmax);
+    atomicMin(bb + 2, ymin);
+    atomicMax(bb + 3, ymax);
+    int* gsum = reinterpret_cast<int*>(&F.pair_gsum[gs]);
+    if (gx) atomicAdd(gsum + 0, gx);
+    if (gy) atomicAdd(gsum + 1, gy);
+    if (pxgx) atomicAdd(&F.pair_pxgx[gs], pxgx);
+}
+__device__ __forceinline__ void flush_agg(const FrameDesc& F, PairTableSmem& T, const Agg& a, uint32_t* status) {
+    int ls = local_insert(T, a.key);
+    if (ls >= 0) {
+        atomicAdd(&T.cnt[ls], a.cnt);
+        atomicMin(&T.xmin[ls], a.xmin);
+        atomicMax(&T.xmax[ls], a.xmax);
+        atomicMin(&T.ymin[ls], a.ymin);
+        atomicMax(&T.ymax[ls], a.ymax);
+        if (a.gx) atomicAdd(&T.gx[ls], a.gx);
+        if (a.gy) atomicAdd(&T.gy[ls], a.gy);
+        if (a.pxgx) atomicAdd(&T.pxgx[ls], (unsigned long long)(long long)a.pxgx);
+    } else {
+        uint32_t gs = global_insert(F, a.key);
+        if (gs == INVALID) {
+            atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
+            return;
+        }
+        global_flush(F, gs, a.cnt, a.xmin, a.xmax, a.ymin, a.ymax, a.gx, a.gy,
+                     (unsigned long long)(long long)a.pxgx);
+    }
+}
+
+// Enumerates the boundary points of pixel (x, y) in the reference's order
+// (find_boundaries.cpp:128-150); lab/big are the CTA's label tile and
+// "component size >= min" flags, (r, c) the pixel's tile coordinates.
+template <typename Emit>
+__device__ __forceinline__ void pixel_points(const uint32_t (*lab)[BP_SW], const uint8_t (*big)[BP_SW], int r, int c,
+                                             uint32_t x, uint32_t y, Emit emit) {
+    const uint32_t p = lab[r][c];
+    const uint32_t cp = p & LABEL_PIXEL_MASK, lp = p & LABEL_VALUE_MASK;
+    const bool bp = big[r][c];
+    auto test = [&](int t, int rr, int cc) {
+        uint32_t q = lab[rr][cc];
+        uint32_t cq = q & LABEL_PIXEL_MASK;
+        if (cq == cp) return;
+        if (!bp || !big[rr][cc]) return;
+        uint32_t lq = q & LABEL_VALUE_MASK;
+        uint32_t px = x | ((uint32_t)t << 14);
+        uint32_t py = cq > cp ? (COLOR_DIR_MASK | y) : y;
+        unsigned long long lo = min(lp, lq), hi = max(lp, lq);
+        emit((lo << 32) | hi, px | (py << 16));
+    };
+    test(0, r, c + 1);
+    {
+        uint32_t left = lab[r][c - 1], down = lab[r + 1][c];
+        bool dup = (left & LABEL_PIXEL_MASK) != (down & LABEL_PIXEL_MASK) && big[r][c - 1] && big[r + 1][c];
+        if (!dup) test(1, r + 1, c - 1);
+    }
+    test(2, r + 1, c);
+    test(3, r + 1, c + 1);
+}
+
+__global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_constant__ FrameSet fs,
+                                                                 uint32_t min_size) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    const int w = F.width, h = F.height;
+    const int ntx = (w + BP_W - 1) / BP_W, nty = (h + BP_H - 1) / BP_H;
+    if ((int)blockIdx.x >= ntx * nty) return;
+    const int x0 = (blockIdx.x % ntx) * BP_W, y0 = (blockIdx.x / ntx) * BP_H;
+    uint32_t* status = F.counters + CNT_STATUS;
+
+    __shared__ uint32_t lab[BP_SH][BP_SW];
+    __shared__ uint8_t big[BP_SH][BP_SW];
+    __shared__ PairTableSmem T;
+    __shared__ uint32_t red[33];
+    __shared__ uint32_t s_base;
+
+    for (int i = threadIdx.x; i < BP_SH * BP_SW; i += blockDim.x) {
+        int r = i / BP_SW, c = i % BP_SW;
+        int y = y0 + r, x = x0 - 1 + c;
+        uint32_t l = (x >= 0 && x < w && y < h) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
+        lab[r][c] = l;
+        big[r][c] = __ldg(F.sizes + (l & LABEL_VALUE_MASK)) >= min_size;
+    }
+    for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
+        T.key[i] = EMPTY_KEY;
+        T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
+        T.gx[i] = 0; T.gy[i] = 0; T.pxgx[i] = 0; T.gslot[i] = INVALID;
+    }
+    __syncthreads();
+
+    const int r = threadIdx.x / (BP_W / 4), c0 = (threadIdx.x % (BP_W / 4)) * 4;
+    const uint32_t y = y0 + r;
+    // pass 1: count and aggregate
+    Agg a0, a1;
+    agg_init(a0, EMPTY_KEY);
+    agg_init(a1, EMPTY_KEY);
+    uint32_t npts = 0;
+    if ((int)y < h) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t x = x0 + c0 + k;
+            if (x == 0 || (int)x >= w) continue;
+            pixel_points(lab, big, r, c0 + k + 1, x, y, [&](unsigned long long key, uint32_t packed) {
+                npts++;
+                if (a0.key == key) { agg_add(a0, packed); return; }
+                if (a1.key == key) { agg_add(a1, packed); return; }
+                if (a0.key == EMPTY_KEY) { agg_init(a0, key); agg_add(a0, packed); return; }
+                if (a1.key != EMPTY_KEY) flush_agg(F, T, a1, status);
+                agg_init(a1, key);
+                agg_add(a1, packed);
+            });
+        }
+    }
+    // warp-level combine of the two running aggregates, then one set of
+    // shared-memory atomics per distinct key per warp
+#pragma unroll
+    for (int s = 0; s < 2; s++) {
+        Agg& a = s == 0 ? a0 : a1;
+        unsigned mask = __match_any_sync(0xffffffffu, a.key);
+        Agg b = a;
+        b.cnt = __reduce_add_sync(mask, a.cnt);
+        b.xmin = __reduce_min_sync(mask, a.xmin);
+        b.xmax = __reduce_max_sync(mask, a.xmax);
+        b.ymin = __reduce_min_sync(mask, a.ymin);
+        b.ymax = __reduce_max_sync(mask, a.ymax);
+        b.gx = __reduce_add_sync(mask, a.gx);
+        b.gy = __reduce_add_sync(mask, a.gy);
+        b.pxgx = __reduce_add_sync(mask, a.pxgx);
+        int leader = __ffs(mask) - 1;
+        if ((int)(threadIdx.x & 31) == leader && a.key != EMPTY_KEY) flush_agg(F, T, b, status);
+    }
+    __syncthreads();
+    // merge the CTA's pairs into the frame's table
+    for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
+        unsigned long long key = T.key[i];
+        if (key == EMPTY_KEY) continue;
+        uint32_t gs = global_insert(F, key);
+        T.gslot[i] = gs;
+        if (gs == INVALID) {
+            atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
+            continue;
+        }
+        global_flush(F, gs, T.cnt[i], T.xmin[i], T.xmax[i], T.ymin[i], T.ymax[i], T.gx[i], T.gy[i], T.pxgx[i]);
+    }
+    // reserve space in the point list
+    uint32_t total;
+    uint32_t off = block_exclusive_scan_u32(npts, red, &total);
+    if (threadIdx.x == 0) {
+        uint32_t b = total ? atomicAdd(F.counters + CNT_POINTS, total) : 0u;
+        if ((unsigned long long)b + total > F.point_cap) atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
+        s_base = b;
+    }
+    __syncthreads();
+    // pass 2: write the points tagged with their pair slot
+    if (npts) {
+        uint32_t pos = s_base + off;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            uint32_t x = x0 + c0 + k;
+            if (x == 0 || (int)x >= w) continue;
+            pixel_points(lab, big, r, c0 + k + 1, x, y, [&](unsigned long long key, uint32_t packed) {
+                int ls = local_lookup(T, key);
+                uint32_t gs = ls >= 0 ? T.gslot[ls] : global_lookup(F, key);
+                if (pos < F.point_cap) F.points[pos] = ((unsigned long long)gs << 32) | packed;
+                pos++;
+            });
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2. pair finalisation: sort keys, filter, cluster indices and extents
+// ---------------------------------------------------------------------------
+constexpr int PF_THREADS = 1024;
+constexpr int PF_SMEM_KEYS = 6144;
+
+__global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_constant__ FrameSet fs,
+                                                               PipelineParams p) {
+    const FrameDesc& F = fs.get(blockIdx.x);
+    uint32_t* status = F.counters + CNT_STATUS;
+    __shared__ unsigned long long s_keys[PF_SMEM_KEYS];
+    __shared__ uint32_t red[33];
+    __shared__ uint32_t s_n;
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    // the sorted key list lives in shared memory when it fits, else in the
+    // frame's cluster_keys buffer's tail (pair_cap entries reserved there)
+    uint32_t npairs_upper = 0;
+    for (uint32_t i = threadIdx.x; i < F.pair_cap; i += blockDim.x) npairs_upper += F.pair_keys[i] != EMPTY_KEY;
+    uint32_t C = block_sum_u32(npairs_upper, red);
+    unsigned long long* keys = C <= (uint32_t)PF_SMEM_KEYS ? s_keys : F.cluster_keys + F.cluster_cap;
+    for (uint32_t i = threadIdx.x; i < F.pair_cap; i += blockDim.x) {
+        unsigned long long k = F.pair_keys[i];
+        if (k != EMPTY_KEY) keys[atomicAdd(&s_n, 1u)] = k;
+    }
+    __syncthreads();
+    bitonic_sort_u64(keys, C);
+    __syncthreads();
+    FilterParams fp;
+    fp.min_cluster_pixels = p.min_cluster_pixels;
+    fp.max_cluster_pixels = 2u * (2u * F.width + 2u * F.height);
+    fp.tag_width = p.tag_width;
+    fp.normal_border = p.normal_border;
+    fp.reversed_border = p.reversed_border;
+    uint32_t carry_start = 0, carry_cluster = 0, carry_fstart = 0;
+    for (uint32_t c0 = 0; c0 < C; c0 += blockDim.x) {
+        uint32_t c = c0 + threadIdx.x;
+        uint32_t slot = INVALID, cnt = 0;
+        bool keep = false;
+        uint4 bb = make_uint4(0, 0, 0, 0);
+        int2 gs = make_int2(0, 0);
+        long long pxgx = 0;
+        if (c < C) {
+            slot = global_lookup(F, keys[c]);
+            cnt = F.pair_count[slot];
+            bb = F.pair_bbox[slot];
+            gs = F.pair_gsum[slot];
+            pxgx = (long long)F.pair_pxgx[slot];
+            keep = valid_blob(fp, cnt, bb.x, bb.y, bb.z, bb.w, gs.x, gs.y, pxgx);
+        }
+        uint32_t tot_cnt, tot_keep, tot_fcnt;
+        uint32_t start = carry_start + block_exclusive_scan_u32(cnt, red, &tot_cnt);
+        uint32_t cid = carry_cluster + block_exclusive_scan_u32(keep ? 1u : 0u, red, &tot_keep);
+        uint32_t fstart = carry_fstart + block_exclusive_scan_u32(keep ? cnt : 0u, red, &tot_fcnt);
+        if (keep) {
+            bool fits = cid < F.cluster_cap && (unsigned long long)fstart + cnt <= F.cpoint_cap;
+            if (!fits) {
+                atomicOr(status, ATAG_DEVFLAG_CLUSTER_OVERFLOW);
+            } else {
+                F.pair_cluster[slot] = cid;
+                F.cluster_keys[cid] = keys[c];
+                atag_cluster_bounds b;
+                b.x_min = (uint16_t)bb.x; b.x_max = (uint16_t)bb.y;
+                b.y_min = (uint16_t)bb.z; b.y_max = (uint16_t)bb.w;
+                b.gx_sum = gs.x; b.gy_sum = gs.y;
+                b.pxgx_pygy_sum = pxgx;
+                b.start = start;
+                b.count = cnt;
+                F.cluster_bounds[cid] = b;
+                F.cluster_extents[cid] = atag_cluster_extents{fstart, cnt};
+                F.cluster_center[cid] = make_float2(bounds_cx(bb.x, bb.y), bounds_cy(bb.z, bb.w));
+                F.cluster_cursor[cid] = 0;
+                F.peak_count[cid] = 0;
+            }
+        }
+        carry_start += tot_cnt;
+        carry_cluster += tot_keep;
+        carry_fstart += tot_fcnt;
+    }
+    if (threadIdx.x == 0) {
+        uint32_t ncl = carry_cluster, npf = carry_fstart;
+        if (ncl > F.cluster_cap) ncl = F.cluster_cap;
+        // clusters are assigned in order, so the kept prefix is [0, ncl)
+        uint32_t np = F.counters[CNT_POINTS];
+        F.counters[CNT_CLUSTERS] = ncl;
+        F.stats->width = F.width;
+        F.stats->height = F.height;
+        F.stats->n_points = np < F.point_cap ? np : F.point_cap;
+        F.stats->n_pairs = C;
+        F.stats->n_clusters = ncl;
+        F.stats->n_cluster_points = npf < F.cpoint_cap ? npf : F.cpoint_cap;
+    }
+}
+
+// Prefix offsets of a per-frame count over the batch (flattened work space
+// for the per-cluster kernels) and reset of the work-queue cursor.
+__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, uint32_t which,
+                                uint32_t* __restrict__ offsets, uint32_t* __restrict__ work_counter) {
+    __shared__ uint32_t red[33];
+    uint32_t carry = 0;
+    for (uint32_t f0 = 0; f0 < n_frames; f0 += blockDim.x) {
+        uint32_t f = f0 + threadIdx.x;
+        uint32_t v = f < n_frames ? fs.get(f).counters[which] : 0u;
+        uint32_t tot;
+        uint32_t e = block_exclusive_scan_u32(v, red, &tot);
+        if (f < n_frames) offsets[f] = carry + e;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        offsets[n_frames] = carry;
+        *work_counter = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. scatter points of surviving pairs into their cluster segments
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_scatter_points(const __grid_constant__ FrameSet fs) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    uint32_t n = F.counters[CNT_POINTS];
+    if (n > F.point_cap) n = F.point_cap;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t cid = INVALID, packed = 0;
+        if (i < n) {
+            unsigned long long e = F.points[i];
+            uint32_t slot = (uint32_t)(e >> 32);
+            packed = (uint32_t)e;
+            if (slot != INVALID) cid = F.pair_cluster[slot];
+        }
+        unsigned mask = __match_any_sync(0xffffffffu, cid);
+        if (cid != INVALID) {
+            int leader = __ffs(mask) - 1;
+            uint32_t b = 0;
+            if ((int)lane == leader) b = atomicAdd(F.cluster_cursor + cid, (uint32_t)__popc(mask));
+            b = __shfl_sync(mask, b, leader);
+            uint32_t rank = __popc(mask & ((1u << lane) - 1u));
+            atag_cluster_extents ext = F.cluster_extents[cid];
+            float2 ctr = F.cluster_center[cid];
+            float theta = calc_theta(packed, ctr.x, ctr.y);
+            uint32_t pos = ext.start + b + rank;
+            F.sortbuf[pos] = ((unsigned long long)float_order_key(theta) << 32) | packed;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. one cluster per CTA: sort, moments, scan, errors, filter, peaks
+// ---------------------------------------------------------------------------
+constexpr int CF_THREADS = 512;
+
+__device__ __forceinline__ long long shfl_up_ll(long long v, int o) {
+    return (long long)__shfl_up_sync(0xffffffffu, (unsigned long long)v, o);
+}
+
+// Block-wide exclusive scan of 6 int64 lanes; returns the thread's prefix.
+__device__ __forceinline__ Moment block_exclusive_scan_moment(const Moment& v, long long (*red)[6]) {
+    long long x[6] = {v.Mx, v.My, v.Mxx, v.Myy, v.Mxy, v.W};
+    long long incl[6];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        long long s = x[j];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long y = shfl_up_ll(s, o);
+            if (lane >= o) s = wadd(s, y);
+        }
+        incl[j] = s;
+    }
+    __syncthreads();
+    if (lane == 31) {
+#pragma unroll
+        for (int j = 0; j < 6; j++) red[wid][j] = incl[j];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int j = 0; j < 6; j++) {
+            long long t = lane < nw ? red[lane][j] : 0;
+            long long s = t;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                long long y = shfl_up_ll(s, o);
+                if (lane >= o) s = wadd(s, y);
+            }
+            if (lane < nw) red[lane][j] = wsub(s, t);  // exclusive warp offsets
+        }
+    }
+    __syncthreads();
+    Moment r;
+    r.Mx = wadd(red[wid][0], wsub(incl[0], x[0]));
+    r.My = wadd(red[wid][1], wsub(incl[1], x[1]));
+    r.Mxx = wadd(red[wid][2], wsub(incl[2], x[2]));
+    r.Myy = wadd(red[wid][3], wsub(incl[3], x[3]));
+    r.Mxy = wadd(red[wid][4], wsub(incl[4], x[4]));
+    r.W = wadd(red[wid][5], wsub(incl[5], x[5]));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t find_frame(const uint32_t* offsets, uint32_t n_frames, uint32_t item) {
+    uint32_t lo = 0, hi = n_frames;  // offsets[lo] <= item < offsets[hi]
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (offsets[mid] <= item) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(CF_THREADS, 1) k_cluster_fit(const __grid_constant__ FrameSet fs,
+                                                             const uint32_t* __restrict__ work_offsets,
+                                                             uint32_t n_frames, uint32_t* __restrict__ work_counter,
+                                                             uint32_t sort_cap) {
+    extern __shared__ unsigned long long smem_keys[];
+    __shared__ long long red_m[32][6];
+    __shared__ unsigned long long red64[32];
+    __shared__ uint32_t red32[33];
+    __shared__ uint32_t s_item;
+    const uint32_t total = work_offsets[n_frames];
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(work_counter, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        if (item >= total) return;
+        const uint32_t fidx = find_frame(work_offsets, n_frames, item);
+        const FrameDesc& F = fs.get(fidx);
+        const uint32_t cid = item - work_offsets[fidx];
+        const atag_cluster_extents ext = F.cluster_extents[cid];
+        const uint32_t n = ext.count, start = ext.start;
+        const bool in_smem = n <= sort_cap;
+        unsigned long long* keys = in_smem ? smem_keys : F.sortbuf + start;
+        if (in_smem)
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) keys[i] = F.sortbuf[start + i];
+        __syncthreads();
+        bitonic_sort_u64(keys, n);
+        __syncthreads();
+        // cluster points, moments and their inclusive scan
+        const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+        const uint32_t i0 = min(n, threadIdx.x * per), i1 = min(n, i0 + per);
+        Moment tot{0, 0, 0, 0, 0, 0};
+        for (uint32_t i = i0; i < i1; i++) {
+            unsigned long long k = keys[i];
+            uint32_t packed = (uint32_t)k;
+            atag_cluster_point cp;
+            cp.packed_x = (uint16_t)packed;
+            cp.packed_y = (uint16_t)(packed >> 16);
+            cp.slope = float_from_order_key((uint32_t)(k >> 32));
+            F.cluster_points[start + i] = cp;
+            tot = m_add(tot, initial_linefit(packed, F.width, F.height, F.grey));
+        }
+        Moment run = block_exclusive_scan_moment(tot, red_m);
+        for (uint32_t i = i0; i < i1; i++) {
+            run = m_add(run, initial_linefit((uint32_t)keys[i], F.width, F.height, F.grey));
+            store_moment(F.line_fit + start + i, run);
+        }
+        __syncthreads();
+        // errors of the windows around each point, then the cyclic filter
+        float* err = in_smem ? reinterpret_cast<float*>(smem_keys) : F.errbuf + 2ull * start;
+        float* flt = err + n;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+            err[i] = window_error(F.line_fit, start, n, (long long)start + i);
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 7; j++) {
+                uint32_t t = (i + n + j - 3) % n;
+                acc = __fadd_rn(acc, __fmul_rn(err[t], filter_tap(j)));
+            }
+            flt[i] = acc;
+        }
+        __syncthreads();
+        // strict local maxima with error != 0 (D10); global point 0 never
+        uint32_t mycount = 0;
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            float cur = flt[i];
+            bool is_max = cur > flt[(i + n - 1) % n] && cur > flt[(i + 1) % n] && cur != 0.0f &&
+                          !(cid == 0 && i == 0);
+            mycount += is_max;
+        }
+        const uint32_t npeaks = block_sum_u32(mycount, red32);
+        // the 10 best by (error desc, index asc): repeated block argmax
+        unsigned long long last = ~0ull;
+        const uint32_t take = npeaks < 10 ? npeaks : 10;
+        for (uint32_t j = 0; j < take; j++) {
+            unsigned long long best = 0;
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+                float cur = flt[i];
+                bool is_max = cur > flt[(i + n - 1) % n] && cur > flt[(i + 1) % n] && cur != 0.0f &&
+                              !(cid == 0 && i == 0);
+                if (!is_max) continue;
+                unsigned long long key = ((unsigned long long)float_order_key(cur) << 32) | (uint32_t)(~i);
+                if (key < last && key > best) best = key;
+            }
+            best = block_max_u64(best, red64);
+            if (threadIdx.x == 0) {
+                atag_corner c;
+                c.line_fit_point_index = ~(uint32_t)best;
+                c.cluster_index = (uint16_t)cid;
+                c.error = float_from_order_key((uint32_t)(best >> 32));
+                F.peaks[(size_t)cid * 10 + j] = c;
+            }
+            last = best;
+        }
+        if (threadIdx.x == 0) F.peak_count[cid] = npeaks;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 5. peak extents (D10-D12), do_indexing + corners, ordered quads
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_peaks_scan(const __grid_constant__ FrameSet fs, PipelineParams p) {
+    const FrameDesc& F = fs.get(blockIdx.x);
+    __shared__ uint32_t red[33];
+    const uint32_t C = F.counters[CNT_CLUSTERS];
+    uint32_t carry_q = 0, carry_k = 0;
+    for (uint32_t c0 = 0; c0 < C; c0 += blockDim.x) {
+        uint32_t c = c0 + threadIdx.x;
+        uint32_t k = c < C ? F.peak_count[c] : 0u;
+        uint32_t tq, tk;
+        uint32_t q = carry_q + block_exclusive_scan_u32(k ? 1u : 0u, red, &tq);
+        uint32_t s = carry_k + block_exclusive_scan_u32(k, red, &tk);
+        if (k) {
+            F.peak_clusters[q] = c;
+            F.peak_extents[q] = atag_peak_extents{s, k};
+        }
+        carry_q += tq;
+        carry_k += tk;
+    }
+    if (threadIdx.x == 0) {
+        F.counters[CNT_PEAKCLU] = carry_q;
+        F.stats->n_corners = carry_k;
+        F.stats->n_peak_clusters = carry_q;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_index_quads(const __grid_constant__ FrameSet fs,
+                                                     const uint32_t* __restrict__ work_offsets, uint32_t n_frames,
+                                                     PipelineParams p) {
+    __shared__ unsigned long long red64[32];
+    __shared__ uint32_t red32[33];
+    const uint32_t total = work_offsets[n_frames];
+    for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
+        const uint32_t fidx = find_frame(work_offsets, n_frames, item);
+        const FrameDesc& F = fs.get(fidx);
+        const uint32_t q = item - work_offsets[fidx];
+        const uint32_t cid = F.peak_clusters[q];
+        const atag_peak_extents pe{0u, F.peak_count[cid]};
+        const atag_cluster_extents ce = F.cluster_extents[p.compat_peak_index ? q : cid];
+        Combination c = evaluate_combination(threadIdx.x, pe, F.peaks + (size_t)cid * 10, F.line_fit + ce.start,
+                                             ce.count, p.max_line_fit_mse, p.cos_critical_f);
+        int chosen = choose_combination(c.err, threadIdx.x, red64, red32);
+        if (chosen < 0) {
+            if (threadIdx.x == 0) {
+                Combination z;
+                for (int s = 0; s < 4; s++) { z.m[s] = Moment{0, 0, 0, 0, 0, 0}; z.nim[s] = 0; z.idx[s] = 0; }
+                write_fitted(F.fitted + q, z);
+                F.quad_ok[q] = 0;
+            }
+        } else if ((int)threadIdx.x == chosen) {
+            write_fitted(F.fitted + q, c);
+            atag_quad_corners qc;
+            bool ok = quad_corners(F.fitted[q], p, q, &qc);
+            F.quad_tmp[q] = qc;
+            F.quad_ok[q] = ok ? 1u : 0u;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_compact_quads(const __grid_constant__ FrameSet fs) {
+    const FrameDesc& F = fs.get(blockIdx.x);
+    __shared__ uint32_t red[33];
+    const uint32_t Cp = F.counters[CNT_PEAKCLU];
+    uint32_t carry = 0, nfit = 0;
+    for (uint32_t c0 = 0; c0 < Cp; c0 += blockDim.x) {
+        uint32_t q = c0 + threadIdx.x;
+        uint32_t ok = q < Cp ? F.quad_ok[q] : 0u;
+        uint32_t fit = 0;
+        if (q < Cp) {
+            const atag_fitted_quad& fq = F.fitted[q];
+            fit = (fq.indices[0] | fq.indices[1] | fq.indices[2] | fq.indices[3]) != 0;
+        }
+        uint32_t tot, tf;
+        uint32_t pos = carry + block_exclusive_scan_u32(ok, red, &tot);
+        block_exclusive_scan_u32(fit, red, &tf);
+        if (ok) {
+            if (pos < F.quad_cap) F.quads[pos] = F.quad_tmp[q];
+        }
+        carry += tot;
+        nfit += tf;
+    }
+    if (threadIdx.x == 0) {
+        if (carry > F.quad_cap) atomicOr(F.counters + CNT_STATUS, ATAG_DEVFLAG_QUAD_OVERFLOW);
+        F.stats->n_fitted = nfit;
+        F.stats->n_quads = carry < F.quad_cap ? carry : F.quad_cap;
+        F.stats->status = F.counters[CNT_STATUS];
+    }
+}
+
+}  // namespace atag

@@ -1,0 +1,381 @@
+// k_pixels.cu — pixel-parallel stages: decimation, adaptive threshold,
+// block-based connected-component labelling and the dense boundary planes.
+//
+// Every kernel takes a FrameDesc table and a blockIdx.y frame index, so the
+// same code serves one frame or a batch of frames of different sizes.
+#include "atag_kernels.cuh"
+
+namespace atag {
+
+// ---------------------------------------------------------------------------
+// a0: point-sampling decimation dst(x, y) = src(f x, f y)
+// ---------------------------------------------------------------------------
+__global__ void k_decimate(const __grid_constant__ FrameSet fs) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    if (F.factor <= 1) return;
+    const uint32_t w = F.width, h = F.height, f = F.factor;
+    const uint32_t words_per_row = w / 4;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words_per_row * h;
+         i += gridDim.x * blockDim.x) {
+        uint32_t y = i / words_per_row, xw = i % words_per_row;
+        const uint8_t* s = F.src + (size_t)y * f * F.src_stride + (size_t)xw * 4 * f;
+        uint32_t v = (uint32_t)s[0] | ((uint32_t)s[f] << 8) | ((uint32_t)s[2 * f] << 16) |
+                     ((uint32_t)s[3 * f] << 24);
+        reinterpret_cast<uint32_t*>(F.grey)[(size_t)y * words_per_row + xw] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// a1: threshold_image (threshold.cpp:8-95) in one kernel.  A CTA owns
+// TH_TX x TH_TY tiles of 4x4 pixels; it loads those plus a one-tile halo
+// into shared memory, takes each tile's min/max, dilates 3x3 (tiles outside
+// the image are neutral, which is the reference's clipping) and thresholds.
+// ---------------------------------------------------------------------------
+constexpr int TH_TX = 32, TH_TY = 8;
+constexpr int TH_EX = TH_TX + 2, TH_EY = TH_TY + 2;
+
+__global__ void __launch_bounds__(256) k_threshold(const __grid_constant__ FrameSet fs,
+                                                   int min_diff, int write_extrema) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    const int tw = F.width / 4, th = F.height / 4;
+    const int ntx = (tw + TH_TX - 1) / TH_TX, nty = (th + TH_TY - 1) / TH_TY;
+    if ((int)blockIdx.x >= ntx * nty) return;
+    const int tx0 = (blockIdx.x % ntx) * TH_TX, ty0 = (blockIdx.x / ntx) * TH_TY;
+
+    __shared__ uint32_t words[TH_EY][TH_EX][4];  // grey rows of each halo tile
+    __shared__ uchar2 ext[TH_EY][TH_EX];
+
+    const uint32_t* g32 = reinterpret_cast<const uint32_t*>(F.grey);
+    const int wpr = F.width / 4;
+    for (int e = threadIdx.x; e < TH_EY * TH_EX; e += blockDim.x) {
+        int ey = e / TH_EX, ex = e % TH_EX;
+        int ty = ty0 + ey - 1, tx = tx0 + ex - 1;
+        uchar2 mm = make_uchar2(255, 0);
+        if (tx >= 0 && tx < tw && ty >= 0 && ty < th) {
+            uint32_t mn = 0xFFFFFFFFu, mx = 0;
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                uint32_t v = __ldg(g32 + (size_t)(ty * 4 + r) * wpr + tx);
+                words[ey][ex][r] = v;
+                mn = __vminu4(mn, v);
+                mx = __vmaxu4(mx, v);
+            }
+            uint32_t a = min(min(mn & 0xFF, (mn >> 8) & 0xFF), min((mn >> 16) & 0xFF, mn >> 24));
+            uint32_t b = max(max(mx & 0xFF, (mx >> 8) & 0xFF), max((mx >> 16) & 0xFF, mx >> 24));
+            mm = make_uchar2((uint8_t)a, (uint8_t)b);
+            if (write_extrema && ex >= 1 && ex <= TH_TX && ey >= 1 && ey <= TH_TY && F.extrema)
+                reinterpret_cast<uchar2*>(F.extrema)[(size_t)ty * tw + tx] = mm;
+        }
+        ext[ey][ex] = mm;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < TH_TX * TH_TY; o += blockDim.x) {
+        int oy = o / TH_TX, ox = o % TH_TX;
+        int ty = ty0 + oy, tx = tx0 + ox;
+        if (tx >= tw || ty >= th) continue;
+        uint32_t mn = 255, mx = 0;
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                uchar2 v = ext[oy + i][ox + j];
+                mn = min(mn, (uint32_t)v.x);
+                mx = max(mx, (uint32_t)v.y);
+            }
+        if (write_extrema && F.filtered_extrema)
+            reinterpret_cast<uchar2*>(F.filtered_extrema)[(size_t)ty * tw + tx] =
+                make_uchar2((uint8_t)mn, (uint8_t)mx);
+        uint32_t comp = (mn + (mx - mn) / 2) & 0xFF;
+        bool flat = (int)(mx - mn) < min_diff;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            uint32_t v = words[oy + 1][ox + 1][r], out = 0;
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                uint32_t p = (v >> (8 * b)) & 0xFF;
+                uint32_t o8 = flat ? 127u : (p > comp ? 255u : 0u);
+                out |= o8 << (8 * b);
+            }
+            reinterpret_cast<uint32_t*>(F.thr)[(size_t)(ty * 4 + r) * wpr + tx] = out;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// a2/a3: BKE connected components (segmentation.cpp:95-392).
+//
+// The reference's partition is the set of connected components of a graph
+// over "slots" (two per 2x2 block: the 255-slot at pixel index y*w+x and the
+// 0-slot at y*w+x+1).  Block C links its 255-slot to the 255-slot of the
+// block holding each neighbour test pixel P(-1,-1), Q(-1,0), Q(-1,1),
+// R(-1,2), S(0,-1), S(1,-1) that is 255 and whose bit survives the
+// `pixels_to_check` mask, and likewise for 0.  The mask is the union over
+// *all* valid (0 or 255) pixels of the block, regardless of colour, which
+// lets a component link through a block of the other colour (:143-171).
+// Roots are the minimum slot index of the set.
+//
+// Here: (1) per CTA tile of CCL_BX x CCL_BY blocks, union-find in shared
+// memory over intra-tile links, then every slot points at its tile-local
+// root (global index) and each tile root holds its tile-local pixel count;
+// (2) links that cross tile borders are merged in global memory;
+// (3) final labels, and tile counts folded into the component root.
+// ---------------------------------------------------------------------------
+constexpr int CCL_BX = 32, CCL_BY = 16;  // blocks per tile (64 x 32 pixels)
+constexpr int CCL_THREADS = CCL_BX * CCL_BY;
+constexpr uint32_t UF_FIND_CAP = 1u << 23;   // longest parent chain followed
+constexpr uint32_t UF_UNION_CAP = 1u << 12;  // retries of one contended union
+
+// Which neighbour blocks (bit 0 P, 1 Q, 2 R, 3 S) a block links to in the
+// 255 forest (wmask) and the 0 forest (bmask); info = pixel colour bits as
+// in BkeBitmap (bits 0-3 = 255 at TL,TR,BL,BR; bits 8-11 = 0).
+struct BlockLinks {
+    uint32_t info, wmask, bmask;
+};
+
+template <typename PixelAt>
+__device__ __forceinline__ BlockLinks block_links(PixelAt px, int x, int y, int w, int h) {
+    uint32_t v00 = px(0, 0), v01 = px(0, 1), v10 = px(1, 0), v11 = px(1, 1);
+    uint32_t info = 0, check = 0;
+    if (v00 == 255) { check |= 0x777; info |= 1; } else if (v00 == 0) { check |= 0x777; info |= 1 << 8; }
+    if (v01 == 255) { check |= 0x777 << 1; info |= 2; } else if (v01 == 0) { check |= 0x777 << 1; info |= 2 << 8; }
+    if (v10 == 255) { check |= 0x777 << 4; info |= 4; } else if (v10 == 0) { check |= 0x777 << 4; info |= 4 << 8; }
+    if (v11 == 255) info |= 8; else if (v11 == 0) info |= 8 << 8;
+    if (x == 0) check &= 0xEEEE; else if (x + 2 >= w) check &= 0x7777;
+    if (y == 0) check &= 0xFFF0; else if (y + 2 >= h) check &= 0x0FFF;
+    uint32_t wm = 0, bm = 0;
+    // test order and neighbour block of each test bit
+    auto test = [&](uint32_t bit, int dy, int dx, uint32_t nb) {
+        if (check & (1u << bit)) {
+            uint32_t t = px(dy, dx);
+            if (t == 255) wm |= nb; else if (t == 0) bm |= nb;
+        }
+    };
+    test(0, -1, -1, 1);
+    test(1, -1, 0, 2);
+    test(2, -1, 1, 2);
+    test(3, -1, 2, 4);
+    test(4, 0, -1, 8);
+    test(8, 1, -1, 8);
+    return BlockLinks{info, wm, bm};
+}
+
+__device__ __forceinline__ uint32_t find_root_volatile(volatile uint32_t* p, uint32_t n) {
+    // path halving: every write replaces a parent by one of its ancestors,
+    // which stays valid under concurrent unions (only roots are re-linked)
+    for (uint32_t it = 0; it < UF_FIND_CAP; it++) {
+        uint32_t q = p[n];
+        if (q == n) return n;
+        uint32_t g = p[q];
+        if (g != q) p[n] = g;
+        n = g;
+    }
+    return n;
+}
+
+// Lock-free union toward the smaller root (union_find.h:50-77) with an
+// iteration cap; returns false if the cap was hit.
+template <typename Ptr>
+__device__ __forceinline__ bool uf_union(Ptr par, uint32_t a, uint32_t b) {
+    for (uint32_t it = 0; it < UF_UNION_CAP; it++) {
+        a = find_root_volatile(par, a);
+        b = find_root_volatile(par, b);
+        if (a == b) return true;
+        if (a < b) {
+            uint32_t old = atomicMin((uint32_t*)&par[b], a);
+            if (old == b) return true;
+            b = old;
+        } else {
+            uint32_t old = atomicMin((uint32_t*)&par[a], b);
+            if (old == a) return true;
+            a = old;
+        }
+    }
+    return false;
+}
+
+__device__ __forceinline__ uint32_t ccl_tiles_x(uint32_t w) { return (w / 2 + CCL_BX - 1) / CCL_BX; }
+__device__ __forceinline__ uint32_t ccl_tiles_y(uint32_t h) { return (h / 2 + CCL_BY - 1) / CCL_BY; }
+
+__global__ void __launch_bounds__(CCL_THREADS) k_ccl_local(const __grid_constant__ FrameSet fs) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    const int w = F.width, h = F.height;
+    const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y(h);
+    if ((int)blockIdx.x >= ntx * nty) return;
+    const int bx0 = (blockIdx.x % ntx) * CCL_BX, by0 = (blockIdx.x / ntx) * CCL_BY;
+    const int x0 = bx0 * 2, y0 = by0 * 2;
+
+    constexpr int PW = 2 * CCL_BX + 2, PH = 2 * CCL_BY + 1;
+    __shared__ uint8_t pix[PH][PW];  // rows y0-1.., cols x0-1..
+    __shared__ uint32_t par[2 * CCL_THREADS];
+    __shared__ uint32_t cnt[2 * CCL_THREADS];
+
+    for (int i = threadIdx.x; i < PH * PW; i += blockDim.x) {
+        int r = i / PW, c = i % PW;
+        int y = y0 - 1 + r, x = x0 - 1 + c;
+        pix[r][c] = (x >= 0 && x < w && y >= 0 && y < h) ? F.thr[(size_t)y * w + x] : 127;
+    }
+    const int tx = threadIdx.x % CCL_BX, ty = threadIdx.x / CCL_BX;
+    const int bx = bx0 + tx, by = by0 + ty;
+    const bool live = bx < w / 2 && by < h / 2;
+    const uint32_t l = threadIdx.x;
+    par[2 * l] = 2 * l;
+    par[2 * l + 1] = 2 * l + 1;
+    cnt[2 * l] = 0;
+    cnt[2 * l + 1] = 0;
+    __syncthreads();
+
+    BlockLinks L{0, 0, 0};
+    if (live) {
+        const int r0 = 2 * ty + 1, c0 = 2 * tx + 1;
+        L = block_links([&](int dy, int dx) { return (uint32_t)pix[r0 + dy][c0 + dx]; }, bx * 2, by * 2, w, h);
+        // intra-tile links
+        const int ndx[4] = {-1, 0, 1, -1}, ndy[4] = {-1, -1, -1, 0};
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+            int ntxl = tx + ndx[n], ntyl = ty + ndy[n];
+            if (ntxl < 0 || ntxl >= CCL_BX || ntyl < 0) continue;
+            uint32_t nl = ntyl * CCL_BX + ntxl;
+            if (L.wmask & (1u << n)) uf_union((volatile uint32_t*)par, 2 * l, 2 * nl);
+            if (L.bmask & (1u << n)) uf_union((volatile uint32_t*)par, 2 * l + 1, 2 * nl + 1);
+        }
+    }
+    __syncthreads();
+    uint32_t rw = find_root_volatile((volatile uint32_t*)par, 2 * l);
+    uint32_t rb = find_root_volatile((volatile uint32_t*)par, 2 * l + 1);
+    if (live) {
+        atomicAdd(&cnt[rw], __popc(L.info & 0xF));
+        atomicAdd(&cnt[rb], __popc(L.info & 0xF00));
+    }
+    __syncthreads();
+    if (live) {
+        auto gslot = [&](uint32_t s) {
+            uint32_t lb = s >> 1;
+            return (uint32_t)((by0 + lb / CCL_BX) * 2) * (uint32_t)w + (uint32_t)(bx0 + lb % CCL_BX) * 2 + (s & 1);
+        };
+        size_t id = (size_t)(by * 2) * w + bx * 2;
+        uint2 parents = make_uint2(gslot(rw), gslot(rb));
+        *reinterpret_cast<uint2*>(F.scratch + id) = parents;
+        uint2 sz = make_uint2(rw == 2 * l ? cnt[2 * l] : 0u, rb == 2 * l + 1 ? cnt[2 * l + 1] : 0u);
+        *reinterpret_cast<uint2*>(F.sizes + id) = sz;
+        *reinterpret_cast<uint2*>(F.sizes + id + w) = make_uint2(0u, 0u);
+        // the reference keeps the block's information word at scratch[id + w]
+        *reinterpret_cast<uint2*>(F.scratch + id + w) = make_uint2(L.info, 0u);
+    }
+}
+
+// Merge the links that cross tile borders: P/Q/R of the tile's top row,
+// P/S of its left column and R (up-right) of its right column.
+constexpr int CCL_BORDER_PER_TILE = CCL_BX + 2 * (CCL_BY - 1);
+
+__global__ void __launch_bounds__(256) k_ccl_border(const __grid_constant__ FrameSet fs) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    const int w = F.width, h = F.height;
+    const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y(h);
+    const int per_tile = CCL_BORDER_PER_TILE;
+    const int total = ntx * nty * per_tile;
+    volatile uint32_t* par = F.scratch;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        int tile = i / per_tile, k = i % per_tile;
+        int tbx = (tile % ntx) * CCL_BX, tby = (tile / ntx) * CCL_BY;
+        int bx, by;
+        if (k < CCL_BX) { bx = tbx + k; by = tby; }
+        else if (k < CCL_BX + CCL_BY - 1) { bx = tbx; by = tby + 1 + (k - CCL_BX); }
+        else { bx = tbx + CCL_BX - 1; by = tby + 1 + (k - CCL_BX - (CCL_BY - 1)); }
+        if (bx >= w / 2 || by >= h / 2) continue;
+        const int x = bx * 2, y = by * 2;
+        const uint8_t* base = F.thr + (size_t)y * w + x;
+        BlockLinks L = block_links([&](int dy, int dx) { return (uint32_t)base[(ptrdiff_t)dy * w + dx]; }, x, y, w, h);
+        const int ndx[4] = {-1, 0, 1, -1}, ndy[4] = {-1, -1, -1, 0};
+        const uint32_t sid = (uint32_t)y * w + x;
+        bool ok = true;
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+            int nbx = bx + ndx[n], nby = by + ndy[n];
+            // same tile?  then it was merged locally
+            if (nbx >= tbx && nbx < tbx + CCL_BX && nby >= tby) continue;
+            uint32_t nid = (uint32_t)(nby * 2) * w + nbx * 2;
+            if (L.wmask & (1u << n)) ok &= uf_union(par, sid, nid);
+            if (L.bmask & (1u << n)) ok &= uf_union(par, sid + 1, nid + 1);
+        }
+        if (!ok && F.counters) atomicOr(F.counters + CNT_STATUS, ATAG_DEVFLAG_UF_ITERATION_CAP);
+    }
+}
+
+// FINAL_LABELLING (segmentation.cpp:316-389): labels, component sizes at
+// the root, parent array compressed to roots.
+__global__ void __launch_bounds__(256) k_ccl_final(const __grid_constant__ FrameSet fs) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    const int w = F.width, h = F.height;
+    const int nbx = w / 2, nb = nbx * (h / 2);
+    volatile uint32_t* par = F.scratch;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
+        int bx = i % nbx, by = i / nbx;
+        size_t id = (size_t)(by * 2) * w + bx * 2;
+        uint32_t sw = (uint32_t)id, sb = (uint32_t)id + 1;
+        uint32_t rw = find_root_volatile(par, sw), rb = find_root_volatile(par, sb);
+        // compress: every slot ends pointing at its root, as the reference's
+        // scratch does after its last compression (segmentation.cpp:309)
+        par[sw] = rw;
+        par[sb] = rb;
+        uint32_t cw = F.sizes[sw], cb = F.sizes[sb];
+        if (rw != sw) {
+            if (cw) atomicAdd(F.sizes + rw, cw);
+            F.sizes[sw] = 0;
+        }
+        if (rb != sb) {
+            if (cb) atomicAdd(F.sizes + rb, cb);
+            F.sizes[sb] = 0;
+        }
+        const uint8_t* t = F.thr + id;
+        uchar2 top = *reinterpret_cast<const uchar2*>(t);
+        uchar2 bot = *reinterpret_cast<const uchar2*>(t + w);
+        auto lab = [&](uint8_t v) { return v == 255 ? (LABEL_PIXEL_MASK | rw) : (v == 0 ? rb : 0u); };
+        *reinterpret_cast<uint2*>(F.labels + id) = make_uint2(lab(top.x), lab(top.y));
+        *reinterpret_cast<uint2*>(F.labels + id + w) = make_uint2(lab(bot.x), lab(bot.y));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// a4: find_boundaries dense planes (find_boundaries.cpp:10-155).  Column 0
+// is never processed (every work-group's local x == 0 is halo-only there),
+// out-of-image neighbours read label 0.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_boundaries_dense(const __grid_constant__ FrameSet fs,
+                                                          uint32_t min_size) {
+    const FrameDesc& F = fs.get(blockIdx.y);
+    const int w = F.width, h = F.height;
+    const size_t N = (size_t)w * h;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x * blockDim.x) {
+        int y = (int)(i / w), x = (int)(i % w);
+        if (x == 0) continue;
+        auto L = [&](int yy, int xx) -> uint32_t {
+            return (xx >= 0 && xx < w && yy >= 0 && yy < h) ? __ldg(F.labels + (size_t)yy * w + xx) : 0u;
+        };
+        uint32_t p = F.labels[i];
+        uint32_t lp = p & LABEL_VALUE_MASK, cp = p & LABEL_PIXEL_MASK;
+        bool small_p = __ldg(F.sizes + lp) < min_size;
+        const int dy[4] = {0, 1, 1, 1}, dx[4] = {1, -1, 0, 1};
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            if (t == 1) {
+                uint32_t left = L(y, x - 1), down = L(y + 1, x);
+                bool dup = (left & LABEL_PIXEL_MASK) != (down & LABEL_PIXEL_MASK) &&
+                           __ldg(F.sizes + (left & LABEL_VALUE_MASK)) >= min_size &&
+                           __ldg(F.sizes + (down & LABEL_VALUE_MASK)) >= min_size;
+                if (dup) continue;
+            }
+            uint32_t q = L(y + dy[t], x + dx[t]);
+            uint32_t cq = q & LABEL_PIXEL_MASK;
+            if (cq == cp) continue;
+            uint32_t lq = q & LABEL_VALUE_MASK;
+            if (small_p || __ldg(F.sizes + lq) < min_size) continue;
+            uint32_t px = (uint32_t)x | ((uint32_t)t << 14);
+            uint32_t py = cq > cp ? (COLOR_DIR_MASK | (uint32_t)y) : (uint32_t)y;
+            uint64_t lo = min(lp, lq), hi = max(lp, lq);
+            reinterpret_cast<uint32_t*>(F.dense_points)[t * N + i] = px | (py << 16);
+            F.dense_keys[t * N + i] = (lo << 32) | hi;
+        }
+    }
+}
+
+}  // namespace atag

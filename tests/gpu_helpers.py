@@ -1,0 +1,112 @@
+"""Shared comparison helpers for the GPU parity tests (oracle vs CUDA)."""
+import numpy as np
+
+CORNER_TOL_PX = 1e-3  # quad corners: max abs difference allowed, pixels
+
+
+def _leaf_bytes(a):
+    """Per-element bytes of every leaf field (padding excluded), so records
+    compare field by field and floats compare by bit pattern."""
+    n = len(a)
+    if a.dtype.names is None:
+        return [np.ascontiguousarray(a).view(np.uint8).reshape(n, -1)] if n else []
+    out = []
+    for name in a.dtype.names:
+        f = a[name]
+        if f.dtype.names is not None:  # nested record (possibly a sub-array of records)
+            out += _leaf_bytes(f.reshape(n, -1).reshape(-1)) if n else []
+            out = [o.reshape(n, -1) for o in out] if n else out
+        else:
+            out.append(np.ascontiguousarray(f).view(np.uint8).reshape(n, -1) if n else None)
+    return [o for o in out if o is not None]
+
+
+def assert_same(a, b, what=""):
+    """Exact (bit-pattern) equality with a short report of where arrays differ."""
+    a, b = np.asarray(a), np.asarray(b)
+    if a.shape != b.shape or a.dtype != b.dtype:
+        raise AssertionError(f"{what}: {a.shape}/{a.dtype} != {b.shape}/{b.dtype}")
+    if a.size == 0:
+        return
+    fa, fb = a.reshape(-1), b.reshape(-1)
+    la, lb = _leaf_bytes(fa), _leaf_bytes(fb)
+    ne = np.zeros(len(fa), bool)
+    for x, y in zip(la, lb):
+        ne |= (x != y).any(axis=1)
+    bad = np.flatnonzero(ne)
+    if len(bad):
+        i = bad[:5]
+        raise AssertionError(f"{what}: {len(bad)} of {fa.size} differ; first at {i.tolist()}: "
+                             f"{fa[i].tolist()} vs {fb[i].tolist()}")
+
+
+def oracle_top10(res):
+    """Per filtered cluster: (peak count, first 10 peaks) from the oracle's
+    sorted corner list."""
+    nclu = len(res["filtered"])
+    counts = np.zeros(nclu, np.uint32)
+    top = {}
+    for pe in res["peak_extents"]:
+        seg = res["corners"][pe["start"]: pe["start"] + pe["count"]]
+        c = int(seg[0]["cluster_index"])
+        counts[c] = pe["count"]
+        top[c] = seg[:10]
+    return counts, top
+
+
+def pair_point_set(views):
+    """GPU boundary points as a sorted array of (key, packed) from the pair
+    table, comparable with the oracle's (keys, points)."""
+    pp = views["pair_points"]
+    slots = (pp >> np.uint64(32)).astype(np.int64)
+    packed = (pp & np.uint64(0xFFFFFFFF)).astype(np.uint64)
+    keys = views["pair_keys"][slots]
+    order = np.lexsort((packed, keys))
+    return keys[order], packed[order]
+
+
+def oracle_point_set(res):
+    p = res["points"]
+    packed = p["packed_x"].astype(np.uint64) | (p["packed_y"].astype(np.uint64) << np.uint64(16))
+    keys = res["keys"]
+    order = np.lexsort((packed, keys))
+    return keys[order], packed[order]
+
+
+def assert_quads_match(gpu_q, ora_q, tol=CORNER_TOL_PX):
+    assert len(gpu_q) == len(ora_q), (len(gpu_q), len(ora_q))
+    if len(gpu_q):
+        d = np.abs(gpu_q["corners"].astype(np.float64) - ora_q["corners"].astype(np.float64))
+        assert np.all(d <= tol), float(d.max())
+        assert np.array_equal(gpu_q["reversed_border"], ora_q["reversed_border"])
+        assert np.array_equal(gpu_q["blob_index"], ora_q["blob_index"])
+
+
+def assert_detect_matches(views, gpu_quads, res, cfg_compat=True):
+    st = views["stats"]
+    assert st["status"] == 0, hex(int(st["status"]))
+    assert (int(st["width"]), int(st["height"])) == (res["width"], res["height"])
+    assert_same(views["thresholded"], res["thresholded"], "thresholded")
+    assert_same(views["labels"], res["labels"], "labels")
+    assert_same(views["sizes"], res["sizes"], "sizes")
+    assert int(st["n_points"]) == len(res["points"])
+    gk, gp = pair_point_set(views)
+    ok, op = oracle_point_set(res)
+    assert np.array_equal(gk, ok) and np.array_equal(gp, op)
+    assert int(st["n_pairs"]) == len(res["bounds"])
+    assert int(st["n_clusters"]) == len(res["filtered"])
+    assert_same(views["cluster_keys"], res["filtered_keys"], "cluster_keys")
+    assert_same(views["cluster_bounds"], res["filtered"], "cluster_bounds")
+    assert_same(views["cluster_extents"], res["extents"], "cluster_extents")
+    assert int(st["n_cluster_points"]) == len(res["cluster_points"])
+    assert_same(views["cluster_points"], res["cluster_points"], "cluster_points")
+    assert_same(views["line_fit"], res["line_fit"], "line_fit")
+    counts, top = oracle_top10(res)
+    assert_same(views["peak_count"], counts, "peak_count")
+    for c, seg in top.items():
+        assert_same(views["peaks"][c][: len(seg)], seg, f"peaks of cluster {c}")
+    assert int(st["n_corners"]) == len(res["corners"])
+    assert int(st["n_peak_clusters"]) == len(res["peak_extents"])
+    assert_same(views["peak_extents"], res["peak_extents"], "peak_extents")
+    assert_same(views["fitted"], res["fitted"], "fitted")
+    assert_quads_match(gpu_quads, res["quads"])

@@ -1,0 +1,82 @@
+"""CPU checks of the C ABI: the library builds/loads, exports every symbol
+include/atag.h declares, records have the reference's sizes, defaults
+match, and calls without a device fail with a status instead of crashing."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from atag import lib, records
+
+
+def test_library_exports_every_declared_symbol():
+    L = lib.load()
+    declared = lib.declared_symbols()
+    assert len(declared) >= 20
+    missing = [s for s in declared if not hasattr(L, s)]
+    assert not missing, missing
+
+
+def test_signature_table_covers_header():
+    assert sorted(lib._SIGNATURES) == lib.declared_symbols()
+
+
+def test_record_sizes_match_reference_layouts():
+    # sizes of the reference's records (probed from its headers)
+    assert records.BOUNDARY_POINT.itemsize == 4
+    assert records.CLUSTER_POINT.itemsize == 8
+    assert records.CLUSTER_BOUNDS.itemsize == 32
+    assert records.LINE_FIT_POINT.itemsize == 64
+    assert records.CORNER.itemsize == 12
+    assert records.FITTED_QUAD.itemsize == 272
+    assert records.QUAD_CORNERS.itemsize == 40
+    assert ctypes.sizeof(records.Config) == 44
+
+
+def test_config_defaults_match_reference_constants():
+    c = lib.default_config()
+    assert (c.decimate, c.min_white_black_diff, c.min_component_size, c.min_cluster_pixels) == (1, 5, 25, 5)
+    assert (c.tag_width, c.normal_border, c.reversed_border) == (4, 1, 0)
+    assert c.max_line_fit_mse == 10.0 and c.critical_angle_deg == 10.0
+    assert c.min_tag_width == 8 and c.compat_peak_index == 1
+
+
+def test_config_defaults_match_oracle():
+    import oracle
+    a, b = lib.default_config(), oracle.default_config()
+    for name, _ in records.Config._fields_:
+        assert getattr(a, name) == getattr(b, name), name
+
+
+def test_status_strings():
+    L = lib.load()
+    for s in range(7):
+        assert L.atag_status_string(s)
+    assert L.atag_status_string(99) == b"unknown status"
+
+
+def test_workspace_size_validates_arguments():
+    L = lib.load()
+    n = ctypes.c_size_t()
+    c = lib.default_config()
+    assert L.atag_workspace_size(ctypes.byref(c), 1920, 1080, 1, 0, ctypes.byref(n)) == 0
+    assert n.value > 1920 * 1080 * 40
+    # odd sizes are refused before anything is launched
+    assert L.atag_workspace_size(ctypes.byref(c), 1922, 1080, 1, 0, ctypes.byref(n)) == 1
+    assert L.atag_workspace_size(ctypes.byref(c), 8192, 1080, 1, 0, ctypes.byref(n)) == 1
+    # batch bound grows with the pixel budget
+    m = ctypes.c_size_t()
+    assert L.atag_workspace_size(ctypes.byref(c), 2592, 1944, 64, 64 * 2592 * 1944, ctypes.byref(m)) == 0
+    assert m.value > n.value
+
+
+def test_calls_without_device_return_status(monkeypatch):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    L = lib.load()
+    st = L.atag_init()
+    assert st == 5  # ATAG_ERR_NO_DEVICE
+    assert L.atag_last_error()
+    st = L.atag_threshold_image(None, None, None, None, 64, 64, None)
+    assert st == 5
