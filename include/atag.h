@@ -284,10 +284,15 @@ typedef struct atag_frame_views {
     const uint8_t *thresholded;                 /* w*h                              */
     const uint32_t *labels;                     /* w*h                              */
     const uint32_t *sizes;                      /* w*h                              */
-    const uint64_t *pair_points;                /* n_points: (pair slot << 32) | packed */
-    const uint64_t *pair_keys;                  /* pair_capacity: slot -> pair key  */
-    uint32_t pair_capacity;
-    uint32_t reserved_;
+    const uint64_t *pair_points;                /* (pair slot << 32) | packed point, for
+                                                   pairs still under the size limit   */
+    uint32_t n_pair_points;                     /* entries in pair_points           */
+    uint32_t pair_capacity;                     /* slots of the pair hash table:    */
+    const uint64_t *pair_keys;                  /*   key (~0 = empty)               */
+    const uint32_t *pair_count;                 /*   points                         */
+    const uint32_t *pair_bbox;                  /*   x_min, x_max, y_min, y_max     */
+    const int32_t *pair_gsum;                   /*   gx_sum, gy_sum                 */
+    const int64_t *pair_pxgx;                   /*   pxgx_pygy_sum                  */
     const uint64_t *cluster_keys;               /* n_clusters pair keys, ascending  */
     const atag_cluster_bounds *cluster_bounds;  /* n_clusters (start = position among
                                                    all pairs' points in key order)  */
@@ -306,6 +311,16 @@ typedef struct atag_frame_views {
 atag_status atag_use_device(int ordinal);
 
 atag_status atag_detector_views(const atag_detector *det, size_t frame, atag_frame_views *out);
+
+/* Stage timing.  When set, every later detect call records events[i] (a
+ * cudaEvent_t) on its stream just before stage i and events[ATAG_STAGE_COUNT]
+ * after the last, so cudaEventElapsedTime(events[i], events[i+1]) is stage
+ * i's device time.  Pass NULL / 0 to stop.  The reference prints cumulative
+ * per-stage wall times instead (src/main.cpp:330-977). */
+#define ATAG_STAGE_COUNT 13
+atag_status atag_detector_set_stage_events(atag_detector *det, void *const *events, size_t n_events);
+/* Name of stage i (e.g. "ccl_local"), or NULL past the last. */
+const char *atag_stage_name(int stage);
 
 #ifdef __cplusplus
 }

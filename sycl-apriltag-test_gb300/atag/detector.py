@@ -94,6 +94,28 @@ class Detector:
                   "atag_detect_host")
         return out[: int(st[0]["n_quads"])], st[0]
 
+    # -- stage timing --------------------------------------------------------
+    def set_stage_events(self, events):
+        """events: lib.STAGE_COUNT + 1 torch.cuda.Event(enable_timing=True)
+        (or None to stop).  Each later enqueue records them between stages."""
+        if not events:
+            lib.check(self.L.atag_detector_set_stage_events(self.handle, None, 0), "set_stage_events")
+            self._stage_events = None
+            return
+        for e in events:  # torch creates the CUDA event on first record
+            e.record()
+        arr = (_P * len(events))(*[e.cuda_event for e in events])
+        lib.check(self.L.atag_detector_set_stage_events(self.handle, arr, len(events)), "set_stage_events")
+        self._stage_events = list(events)
+
+    def stage_times_ms(self):
+        """Per-stage device times of the last enqueue (needs set_stage_events;
+        synchronises on the last event)."""
+        ev = self._stage_events
+        ev[-1].synchronize()
+        return {lib.load().atag_stage_name(i).decode(): ev[i].elapsed_time(ev[i + 1])
+                for i in range(len(ev) - 1)}
+
     # -- intermediates -------------------------------------------------------
     def _dev_bytes(self, ptr, nbytes):
         if nbytes == 0 or not ptr:
@@ -116,7 +138,8 @@ class Detector:
         w, h = int(st["width"]), int(st["height"])
         N = w * h
         ncl, npf, ncp = int(st["n_clusters"]), int(st["n_cluster_points"]), int(st["n_peak_clusters"])
-        npts = int(st["n_points"])
+        npts = int(v.n_pair_points)
+        pc = int(v.pair_capacity)
         g = self._dev_bytes
         return {
             "stats": st,
@@ -125,7 +148,11 @@ class Detector:
             "labels": g(v.labels, 4 * N).view(np.uint32).reshape(h, w),
             "sizes": g(v.sizes, 4 * N).view(np.uint32),
             "pair_points": g(v.pair_points, 8 * npts).view(np.uint64),
-            "pair_keys": g(v.pair_keys, 8 * v.pair_capacity).view(np.uint64),
+            "pair_keys": g(v.pair_keys, 8 * pc).view(np.uint64),
+            "pair_count": g(v.pair_count, 4 * pc).view(np.uint32),
+            "pair_bbox": g(v.pair_bbox, 16 * pc).view(np.uint32).reshape(pc, 4),
+            "pair_gsum": g(v.pair_gsum, 8 * pc).view(np.int32).reshape(pc, 2),
+            "pair_pxgx": g(v.pair_pxgx, 8 * pc).view(np.int64),
             "cluster_keys": g(v.cluster_keys, 8 * ncl).view(np.uint64),
             "cluster_bounds": g(v.cluster_bounds, 32 * ncl).view(CLUSTER_BOUNDS),
             "cluster_extents": g(v.cluster_extents, 8 * ncl).view(CLUSTER_EXTENTS),

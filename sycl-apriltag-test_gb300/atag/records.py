@@ -43,9 +43,9 @@ class Frame(ctypes.Structure):
 
 
 class FrameViews(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_void_p) for n in ("decimated", "thresholded", "labels", "sizes", "pair_points",
-                                                "pair_keys")] + \
-               [("pair_capacity", ctypes.c_uint32), ("reserved_", ctypes.c_uint32)] + \
+    _fields_ = [(n, ctypes.c_void_p) for n in ("decimated", "thresholded", "labels", "sizes", "pair_points")] + \
+               [("n_pair_points", ctypes.c_uint32), ("pair_capacity", ctypes.c_uint32)] + \
+               [(n, ctypes.c_void_p) for n in ("pair_keys", "pair_count", "pair_bbox", "pair_gsum", "pair_pxgx")] + \
                [(n, ctypes.c_void_p) for n in ("cluster_keys", "cluster_bounds", "cluster_extents",
                                                 "cluster_points", "line_fit_points", "peak_count", "peaks",
                                                 "peak_clusters", "peak_extents", "fitted")]

@@ -166,6 +166,27 @@ __device__ __forceinline__ Moment initial_linefit(uint32_t packed, uint32_t widt
     return Moment{W * rx, W * ry, W * rx * rx, W * ry * ry, W * rx * ry, W};
 }
 
+// The inputs of compute_initial_linefit packed as rx | ry << 16 | W << 32
+// (rx, ry <= 8193, W <= 362), so a cluster's moments can be rebuilt from
+// shared memory without touching the image again.
+__device__ __forceinline__ unsigned long long linefit_rxyw(uint32_t packed, uint32_t width, uint32_t height,
+                                                           const uint8_t* __restrict__ grey) {
+    uint32_t rx = bp_xd(packed) + 1;
+    uint32_t ry = bp_yd(packed) + 1;
+    uint32_t x = rx / 2, y = rx / 2;
+    uint32_t W = 1;
+    if (x > 0 && x + 1 < width && y > 0 && y + 1 < height) {
+        int gx = (int)__ldg(grey + (size_t)y * width + x + 1) - (int)__ldg(grey + (size_t)y * width + x - 1);
+        int gy = (int)__ldg(grey + (size_t)(y + 1) * width + x) - (int)__ldg(grey + (size_t)(y - 1) * width + x);
+        W += isqrt_small((uint32_t)(gx * gx + gy * gy));
+    }
+    return (unsigned long long)rx | ((unsigned long long)ry << 16) | ((unsigned long long)W << 32);
+}
+__device__ __forceinline__ Moment moment_of(unsigned long long v) {
+    long long rx = (long long)(v & 0xFFFF), ry = (long long)((v >> 16) & 0xFFFF), W = (long long)(v >> 32);
+    return Moment{W * rx, W * ry, W * rx * rx, W * ry * ry, W * rx * ry, W};
+}
+
 // get_moment, fit_quad.cpp:15-35 over a prefix-sum array of one cluster.
 __device__ __forceinline__ Moment get_moment(const atag_line_fit_point* points, unsigned long long n,
                                              unsigned long long i0, unsigned long long i1,
@@ -232,6 +253,20 @@ __device__ __forceinline__ float window_error(const atag_line_fit_point* points,
     Moment m = get_moment(points + start, count, i0, i1, &n);
     float e;
     fit_line(m, n, nullptr, &e, nullptr);
+    return e;
+}
+
+// window_error for a point at cluster-local index i of a cluster of n > 2k
+// points whose prefix sums start at `points` (same arithmetic, no modulo).
+__device__ __forceinline__ float window_error_local(const atag_line_fit_point* points, uint32_t n, uint32_t k,
+                                                    uint32_t i) {
+    if (k < 2) return __int_as_float(0x7fc00000);
+    uint32_t i0 = i >= k ? i - k : i + n - k;
+    uint32_t i1 = i + k < n ? i + k : i + k - n;
+    unsigned long long cnt;
+    Moment m = get_moment(points, n, i0, i1, &cnt);
+    float e;
+    fit_line(m, cnt, nullptr, &e, nullptr);
     return e;
 }
 
@@ -387,6 +422,73 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_u32(uint32_t v, uint32_
     uint32_t r = red[wid] + x - v;
     *total = red[32];
     return r;
+}
+
+// Stable LSD radix sort of n 64-bit keys, 8 bits per pass.  Each warp owns a
+// contiguous range of the input so the scatter keeps input order within a
+// digit.  `hist` holds (blockDim/32) x 256 counters, `red` 33 slots.
+// Passes where every key has the same digit are skipped.  Returns the
+// buffer that holds the sorted keys (a or b).
+__device__ __forceinline__ unsigned long long* block_radix_sort_u64(unsigned long long* a, unsigned long long* b,
+                                                                   uint32_t n, uint32_t* hist, uint32_t* red,
+                                                                   uint32_t* s_flag) {
+    const uint32_t W = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t lo = (uint32_t)((unsigned long long)n * w / W), hi = (uint32_t)((unsigned long long)n * (w + 1) / W);
+    for (int pass = 0; pass < 8; pass++) {
+        const int sh = pass * 8;
+        __syncthreads();  // every thread is done with the previous pass's flag and counters
+        for (uint32_t i = threadIdx.x; i < W * 256; i += blockDim.x) hist[i] = 0;
+        if (threadIdx.x == 0) *s_flag = 0;
+        __syncthreads();
+        for (uint32_t i = lo + lane; i < hi; i += 32) atomicAdd(&hist[w * 256 + (uint32_t)((a[i] >> sh) & 255)], 1u);
+        __syncthreads();
+        if (threadIdx.x < 256) {
+            uint32_t t = 0;
+            for (uint32_t ww = 0; ww < W; ww++) t += hist[ww * 256 + threadIdx.x];
+            if (t == n) *s_flag = 1;  // all keys share this digit: the pass is the identity
+        }
+        __syncthreads();
+        if (*s_flag) continue;
+        // exclusive scan in (digit, warp) order; 8 consecutive entries per thread
+        uint32_t vals[8], sum = 0;
+        const uint32_t L0 = threadIdx.x * 8;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            uint32_t L = L0 + e, d = L / W, ww = L % W;
+            vals[e] = hist[ww * 256 + d];
+            sum += vals[e];
+        }
+        uint32_t total;
+        uint32_t run = block_exclusive_scan_u32(sum, red, &total);
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            uint32_t L = L0 + e, d = L / W, ww = L % W;
+            hist[ww * 256 + d] = run;
+            run += vals[e];
+        }
+        __syncthreads();
+        for (uint32_t base = lo; base < hi; base += 32) {
+            const uint32_t i = base + lane;
+            const bool v = i < hi;
+            const unsigned long long key = v ? a[i] : 0ull;
+            const uint32_t d = v ? (uint32_t)((key >> sh) & 255) : 256u;
+            const unsigned m = __match_any_sync(0xffffffffu, d);
+            const uint32_t rank = __popc(m & ((1u << lane) - 1u));
+            const uint32_t p = v ? hist[w * 256 + d] : 0u;
+            __syncwarp();
+            if (v) {
+                b[p + rank] = key;
+                if ((int)lane == __ffs(m) - 1) hist[w * 256 + d] = p + __popc(m);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        unsigned long long* t = a;
+        a = b;
+        b = t;
+    }
+    return a;
 }
 
 }  // namespace atag

@@ -56,6 +56,7 @@ struct FrameDesc {
     atag_cluster_point* cluster_points;
     atag_line_fit_point* line_fit;
     float* errbuf;                     // 2 floats per point (big clusters)
+    uint32_t* cluster_work;            // small clusters from the front, large from the back
     // outputs
     atag_quad_corners* quads;
     uint32_t quad_cap;
@@ -79,8 +80,21 @@ enum Counter : uint32_t {
     CNT_CLUSTERS = 2,    // filtered clusters
     CNT_PEAKCLU = 3,     // clusters with peaks
     CNT_WORK = 4,        // work-queue cursor
+    CNT_ALLPOINTS = 5,   // boundary points found (list entries of pairs already
+                         // known to exceed the cluster size limit are skipped)
+    CNT_SMALL = 6,       // clusters of at most CF_SMALL_CAP points
+    CNT_LARGE = 7,       // larger clusters
     CNT_COUNT = 8
 };
+
+// Cluster-fit kernel shapes: most clusters are small and run several per SM
+// (bitonic sort in 32 KB of shared memory); large ones get a 512-thread CTA
+// with two 96 KB key buffers for a radix sort plus its histograms.  Larger
+// clusters than CF_LARGE_CAP sort in global memory.
+constexpr uint32_t CF_SMALL_THREADS = 128, CF_SMALL_CAP = 4096;
+constexpr uint32_t CF_LARGE_THREADS = 512, CF_LARGE_CAP = 12288;
+constexpr uint32_t CF_SMALL_SMEM = CF_SMALL_CAP * 8;
+constexpr uint32_t CF_LARGE_SMEM = 2 * CF_LARGE_CAP * 8 + (CF_LARGE_THREADS / 32) * 256 * 4;
 
 struct PipelineParams {
     int min_white_black_diff;
@@ -117,11 +131,13 @@ __global__ void k_reset_frames(const __grid_constant__ FrameSet fs);
 __global__ void k_boundaries_pairs(const __grid_constant__ FrameSet fs, uint32_t min_size);
 __global__ void k_pairs_finalize(const __grid_constant__ FrameSet fs, PipelineParams p);
 __global__ void k_scatter_points(const __grid_constant__ FrameSet fs);
-__global__ void k_cluster_fit(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets, uint32_t n_frames,
-                              uint32_t* work_counter, uint32_t sort_cap);
+__global__ void k_cluster_fit_small(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets,
+                                    uint32_t n_frames, uint32_t* work_counter);
+__global__ void k_cluster_fit_large(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets,
+                                    uint32_t n_frames, uint32_t* work_counter);
 __global__ void k_peaks_scan(const __grid_constant__ FrameSet fs, PipelineParams p);
-__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, uint32_t which,
-                                uint32_t* offsets, uint32_t* work_counters);
+__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, uint32_t which0,
+                                uint32_t* offsets0, uint32_t which1, uint32_t* offsets1, uint32_t* work_counters);
 __global__ void k_index_quads(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets, uint32_t n_frames,
                               PipelineParams p);
 __global__ void k_compact_quads(const __grid_constant__ FrameSet fs);

@@ -50,7 +50,6 @@ struct DeviceInfo {
 std::mutex g_init_mutex;
 DeviceInfo g_dev[64];
 
-constexpr uint32_t SORT_CAP = 12288;  // cluster points sorted in shared memory (96 KB)
 
 atag_status ensure_device(DeviceInfo** out) {
     int dev = 0;
@@ -68,8 +67,7 @@ atag_status ensure_device(DeviceInfo** out) {
         cudaFuncAttributes fa;
         e = cudaFuncGetAttributes(&fa, k_threshold);
         if (e != cudaSuccess) return fail(ATAG_ERR_NO_DEVICE, "kernels do not load: %s", cudaGetErrorString(e));
-        CK(cudaFuncSetAttribute(k_cluster_fit, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(SORT_CAP * sizeof(unsigned long long))));
+        CK(cudaFuncSetAttribute(k_cluster_fit_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF_LARGE_SMEM));
         d.num_sms = prop.multiProcessorCount;
         d.smem_optin = prop.sharedMemPerBlockOptin;
         d.device = dev;
@@ -188,6 +186,7 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, FrameDe
     f.cluster_points = (atag_cluster_point*)take(sizeof(atag_cluster_point) * c.cpoint_cap);
     f.line_fit = (atag_line_fit_point*)take(sizeof(atag_line_fit_point) * c.cpoint_cap);
     f.errbuf = (float*)take(8ull * c.cpoint_cap);
+    f.cluster_work = (uint32_t*)take(4ull * c.cluster_cap);
     f.counters = (uint32_t*)take(4ull * CNT_COUNT);
     if (d) *d = f;
     return off;
@@ -210,7 +209,9 @@ struct atag_detector {
     bool owns_ws = false;
     // header carve-out
     FrameDesc* d_tables = nullptr;   // RING x max_frames
-    uint32_t* d_work = nullptr;      // offsets (2 x (max_frames + 1)) + 2 counters
+    uint32_t* d_work = nullptr;      // offsets (3 x (max_frames + 1)) + 3 counters
+    cudaStream_t side = nullptr;     // second stream for the large-cluster kernel
+    cudaEvent_t fork = nullptr, join = nullptr;
     uint8_t* d_input = nullptr;      // host-upload input region
     size_t input_bytes = 0;
     atag_quad_corners* d_hquads = nullptr;  // host-path quad staging
@@ -225,6 +226,7 @@ struct atag_detector {
     int last_slot = -1;
     std::vector<FrameDesc> last;     // table last uploaded
     std::vector<FrameDesc> cur;      // table of the last call
+    std::vector<cudaEvent_t> stage_events;
 };
 
 namespace {
@@ -234,7 +236,7 @@ constexpr size_t HOST_QUAD_CAP = 4096;
 size_t header_bytes(size_t max_frames, size_t input_bytes) {
     size_t b = 0;
     b += al(sizeof(FrameDesc) * RING * max_frames);
-    b += al(4 * (2 * (max_frames + 1) + 2));
+    b += al(4 * (3 * (max_frames + 1) + 3));
     b += al(input_bytes);
     b += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
     b += al(sizeof(atag_frame_stats));
@@ -462,7 +464,7 @@ atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t ma
     }
     char* p = det->ws;
     det->d_tables = (FrameDesc*)p; p += al(sizeof(FrameDesc) * RING * max_frames);
-    det->d_work = (uint32_t*)p; p += al(4 * (2 * (max_frames + 1) + 2));
+    det->d_work = (uint32_t*)p; p += al(4 * (3 * (max_frames + 1) + 3));
     det->input_bytes = max_total_pixels * (size_t)c.decimate * (size_t)c.decimate;
     det->d_input = (uint8_t*)p; p += al(det->input_bytes);
     det->d_hquads = (atag_quad_corners*)p; p += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
@@ -477,6 +479,9 @@ atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t ma
         return fail(ATAG_ERR_OUT_OF_MEMORY, "cudaHostAlloc: %s", cudaGetErrorString(e));
     }
     for (int i = 0; i < RING; i++) cudaEventCreateWithFlags(&det->ev[i], cudaEventDisableTiming);
+    cudaStreamCreateWithFlags(&det->side, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&det->fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&det->join, cudaEventDisableTiming);
     *out = det;
     return ATAG_OK;
 }
@@ -487,6 +492,12 @@ atag_status atag_detector_destroy(atag_detector* det) {
         cudaEventSynchronize(det->ev[i]);
         cudaEventDestroy(det->ev[i]);
     }
+    if (det->side) {
+        cudaStreamSynchronize(det->side);
+        cudaStreamDestroy(det->side);
+    }
+    if (det->fork) cudaEventDestroy(det->fork);
+    if (det->join) cudaEventDestroy(det->join);
     if (det->h_staging) cudaFreeHost(det->h_staging);
     if (det->owns_ws) cudaFree(det->ws);
     delete det;
@@ -555,38 +566,74 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     fs.table = d_table;
     const PipelineParams& p = det->pp;
     const int sms = det->dev->num_sms;
-    uint32_t* off_clusters = det->d_work;
-    uint32_t* off_peaks = det->d_work + (n + 1);
-    uint32_t* wc = det->d_work + 2 * (det->max_frames + 1);
+    uint32_t* off_small = det->d_work;
+    uint32_t* off_large = det->d_work + (n + 1);
+    uint32_t* off_peaks = det->d_work + 2 * (n + 1);
+    uint32_t* wc = det->d_work + 3 * (det->max_frames + 1);
 
+    const bool timed = det->stage_events.size() == ATAG_STAGE_COUNT + 1;
+    auto mark = [&](int i) -> atag_status {
+        if (timed) CK(cudaEventRecord(det->stage_events[i], s));
+        return ATAG_OK;
+    };
+#define STAGE(i) do { atag_status m_ = mark(i); if (m_) return m_; } while (0)
+    const size_t tiles_ccl = cdiv(mw / 2, 32) * cdiv(mh / 2, 16);
+    STAGE(0);
     k_reset_frames<<<grid2(cdiv(max_pair, 256), n), 256, 0, s>>>(fs);
     LAUNCHED();
+    STAGE(1);
     if (any_decim) {
         k_decimate<<<grid2(std::min<size_t>(cdiv(mw / 4 * mh, 256), 2048), n), 256, 0, s>>>(fs);
         LAUNCHED();
     }
+    STAGE(2);
     k_threshold<<<grid2(cdiv(mw / 4, 32) * cdiv(mh / 4, 8), n), 256, 0, s>>>(fs, p.min_white_black_diff, 0);
     LAUNCHED();
-    st = launch_segmentation(fs, mw, mh, n, s);
-    if (st) return st;
+    STAGE(3);
+    k_ccl_local<<<grid2(tiles_ccl, n), 512, 0, s>>>(fs);
+    LAUNCHED();
+    STAGE(4);
+    k_ccl_border<<<grid2(cdiv(tiles_ccl * (32 + 2 * (16 - 1)), 256), n), 256, 0, s>>>(fs);
+    LAUNCHED();
+    STAGE(5);
+    k_ccl_final<<<grid2(std::min<size_t>(cdiv((mw / 2) * (mh / 2), 256), 8192), n), 256, 0, s>>>(fs);
+    LAUNCHED();
+    STAGE(6);
     k_boundaries_pairs<<<grid2(cdiv(mw, 64) * cdiv(mh, 16), n), 256, 0, s>>>(fs, p.min_component_size);
     LAUNCHED();
+    STAGE(7);
     k_pairs_finalize<<<(unsigned)n, 1024, 0, s>>>(fs, p);
     LAUNCHED();
-    k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_CLUSTERS, off_clusters, wc);
+    k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_SMALL, off_small, CNT_LARGE, off_large, wc);
     LAUNCHED();
+    STAGE(8);
     k_scatter_points<<<grid2(std::min<size_t>(cdiv(max_points, 256), 1024), n), 256, 0, s>>>(fs);
     LAUNCHED();
-    k_cluster_fit<<<sms, 512, SORT_CAP * sizeof(unsigned long long), s>>>(fs, off_clusters, (uint32_t)n, wc, SORT_CAP);
+    STAGE(9);
+    // large clusters on the side stream, concurrently with the small ones
+    CK(cudaEventRecord(det->fork, s));
+    CK(cudaStreamWaitEvent(det->side, det->fork, 0));
+    k_cluster_fit_large<<<std::max(1, sms / 4), CF_LARGE_THREADS, CF_LARGE_SMEM, det->side>>>(fs, off_large,
+                                                                                                (uint32_t)n, wc + 1);
     LAUNCHED();
+    k_cluster_fit_small<<<sms * 4, CF_SMALL_THREADS, CF_SMALL_SMEM, s>>>(
+        fs, off_small, (uint32_t)n, wc);
+    LAUNCHED();
+    CK(cudaEventRecord(det->join, det->side));
+    CK(cudaStreamWaitEvent(s, det->join, 0));
+    STAGE(10);
     k_peaks_scan<<<(unsigned)n, 1024, 0, s>>>(fs, p);
     LAUNCHED();
-    k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_PEAKCLU, off_peaks, wc + 1);
+    k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_PEAKCLU, off_peaks, 0, nullptr, wc + 2);
     LAUNCHED();
+    STAGE(11);
     k_index_quads<<<sms * 8, 256, 0, s>>>(fs, off_peaks, (uint32_t)n, p);
     LAUNCHED();
+    STAGE(12);
     k_compact_quads<<<(unsigned)n, 1024, 0, s>>>(fs);
     LAUNCHED();
+    STAGE(13);
+#undef STAGE
     return ATAG_OK;
 }
 
@@ -620,8 +667,16 @@ atag_status atag_detector_views(const atag_detector* det, size_t frame, atag_fra
     out->labels = d.labels;
     out->sizes = d.sizes;
     out->pair_points = (const uint64_t*)d.points;
-    out->pair_keys = (const uint64_t*)d.pair_keys;
+    uint32_t n_list = 0;
+    if (cudaMemcpy(&n_list, d.counters + CNT_POINTS, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(ATAG_ERR_CUDA, "detector_views: reading the point count failed");
+    out->n_pair_points = n_list < d.point_cap ? n_list : d.point_cap;
     out->pair_capacity = d.pair_cap;
+    out->pair_keys = (const uint64_t*)d.pair_keys;
+    out->pair_count = d.pair_count;
+    out->pair_bbox = (const uint32_t*)d.pair_bbox;
+    out->pair_gsum = (const int32_t*)d.pair_gsum;
+    out->pair_pxgx = (const int64_t*)d.pair_pxgx;
     out->cluster_keys = (const uint64_t*)d.cluster_keys;
     out->cluster_bounds = d.cluster_bounds;
     out->cluster_extents = d.cluster_extents;
@@ -633,6 +688,23 @@ atag_status atag_detector_views(const atag_detector* det, size_t frame, atag_fra
     out->peak_extents = d.peak_extents;
     out->fitted = d.fitted;
     return ATAG_OK;
+}
+
+atag_status atag_detector_set_stage_events(atag_detector* det, void* const* events, size_t n) {
+    if (!det) return fail(ATAG_ERR_INVALID_ARGUMENT, "set_stage_events: null detector");
+    det->stage_events.clear();
+    if (!events || n == 0) return ATAG_OK;
+    if (n != ATAG_STAGE_COUNT + 1)
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "set_stage_events: need %d events, got %zu", ATAG_STAGE_COUNT + 1, n);
+    for (size_t i = 0; i < n; i++) det->stage_events.push_back((cudaEvent_t)events[i]);
+    return ATAG_OK;
+}
+
+const char* atag_stage_name(int i) {
+    static const char* names[ATAG_STAGE_COUNT] = {
+        "reset", "decimate", "threshold", "ccl_local", "ccl_border", "ccl_final", "boundaries_pairs",
+        "pairs_finalize", "scatter_points", "cluster_fit", "peaks_scan", "index_quads", "compact_quads"};
+    return (i >= 0 && i < ATAG_STAGE_COUNT) ? names[i] : nullptr;
 }
 
 atag_status atag_use_device(int ordinal) {

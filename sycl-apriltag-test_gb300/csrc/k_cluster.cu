@@ -57,27 +57,6 @@ constexpr int BP_SW = BP_W + 2, BP_SH = BP_H + 1;
 constexpr int BP_LC = 256;                     // CTA hash-table entries
 constexpr int BP_THREADS = 256;                // 4 pixels per thread
 
-struct Agg {
-    unsigned long long key;
-    uint32_t cnt, xmin, xmax, ymin, ymax;
-    int gx, gy, pxgx;
-};
-
-__device__ __forceinline__ void agg_init(Agg& a, unsigned long long key) {
-    a.key = key;
-    a.cnt = 0; a.xmin = 0xFFFFFFFFu; a.xmax = 0; a.ymin = 0xFFFFFFFFu; a.ymax = 0;
-    a.gx = 0; a.gy = 0; a.pxgx = 0;
-}
-__device__ __forceinline__ void agg_add(Agg& a, uint32_t packed) {
-    uint32_t xd = bp_xd(packed), yd = bp_yd(packed);
-    int gx = bp_gx(packed), gy = bp_gy(packed);
-    a.cnt += 1;
-    a.xmin = min(a.xmin, xd); a.xmax = max(a.xmax, xd);
-    a.ymin = min(a.ymin, yd); a.ymax = max(a.ymax, yd);
-    a.gx += gx; a.gy += gy;
-    a.pxgx += (int)xd * gx + (int)yd * gy;
-}
-
 struct PairTableSmem {
     unsigned long long key[BP_LC];
     uint32_t cnt[BP_LC], xmin[BP_LC], xmax[BP_LC], ymin[BP_LC], ymax[BP_LC];
@@ -86,21 +65,17 @@ struct PairTableSmem {
     uint32_t gslot[BP_LC];
 };
 
+// Insert-or-find in the CTA's pair table; a plain read first avoids the
+// atomic for keys that are already present (the common case).
 __device__ __forceinline__ int local_insert(PairTableSmem& T, unsigned long long key) {
     uint32_t h = hash_key(key) & (BP_LC - 1);
     for (int p = 0; p < BP_LC; p++) {
-        unsigned long long k = atomicCAS(&T.key[h], EMPTY_KEY, key);
-        if (k == EMPTY_KEY || k == key) return (int)h;
-        h = (h + 1) & (BP_LC - 1);
-    }
-    return -1;
-}
-__device__ __forceinline__ int local_lookup(const PairTableSmem& T, unsigned long long key) {
-    uint32_t h = hash_key(key) & (BP_LC - 1);
-    for (int p = 0; p < BP_LC; p++) {
-        unsigned long long k = T.key[h];
+        unsigned long long k = *(volatile unsigned long long*)&T.key[h];
         if (k == key) return (int)h;
-        if (k == EMPTY_KEY) return -1;
+        if (k == EMPTY_KEY) {
+            k = atomicCAS(&T.key[h], EMPTY_KEY, key);
+            if (k == EMPTY_KEY || k == key) return (int)h;
+        }
         h = (h + 1) & (BP_LC - 1);
     }
     return -1;
@@ -124,10 +99,10 @@ __device__ __forceinline__ uint32_t global_lookup(const FrameDesc& F, unsigned l
     }
     return INVALID;
 }
-__device__ __forceinline__ void global_flush(const FrameDesc& F, uint32_t gs, uint32_t cnt, uint32_t xmin,
-                                             uint32_t xmax, uint32_t ymin, uint32_t ymax, int gx, int gy,
-                                             unsigned long long pxgx) {
-    atomicAdd(&F.pair_count[gs], cnt);
+__device__ __forceinline__ uint32_t global_flush(const FrameDesc& F, uint32_t gs, uint32_t cnt, uint32_t xmin,
+                                                 uint32_t xmax, uint32_t ymin, uint32_t ymax, int gx, int gy,
+                                                 unsigned long long pxgx) {
+    uint32_t old = atomicAdd(&F.pair_count[gs], cnt);
     uint32_t* bb = reinterpret_cast<uint32_t*>(&F.pair_bbox[gs]);
     atomicMin(bb + 0, xmin);
     atomicMax(bb + 1, xmax);
@@ -137,59 +112,22 @@ __device__ __forceinline__ void global_flush(const FrameDesc& F, uint32_t gs, ui
     if (gx) atomicAdd(gsum + 0, gx);
     if (gy) atomicAdd(gsum + 1, gy);
     if (pxgx) atomicAdd(&F.pair_pxgx[gs], pxgx);
-}
-__device__ __forceinline__ void flush_agg(const FrameDesc& F, PairTableSmem& T, const Agg& a, uint32_t* status) {
-    int ls = local_insert(T, a.key);
-    if (ls >= 0) {
-        atomicAdd(&T.cnt[ls], a.cnt);
-        atomicMin(&T.xmin[ls], a.xmin);
-        atomicMax(&T.xmax[ls], a.xmax);
-        atomicMin(&T.ymin[ls], a.ymin);
-        atomicMax(&T.ymax[ls], a.ymax);
-        if (a.gx) atomicAdd(&T.gx[ls], a.gx);
-        if (a.gy) atomicAdd(&T.gy[ls], a.gy);
-        if (a.pxgx) atomicAdd(&T.pxgx[ls], (unsigned long long)(long long)a.pxgx);
-    } else {
-        uint32_t gs = global_insert(F, a.key);
-        if (gs == INVALID) {
-            atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
-            return;
-        }
-        global_flush(F, gs, a.cnt, a.xmin, a.xmax, a.ymin, a.ymax, a.gx, a.gy,
-                     (unsigned long long)(long long)a.pxgx);
-    }
+    return old;
 }
 
-// Enumerates the boundary points of pixel (x, y) in the reference's order
-// (find_boundaries.cpp:128-150); lab/big are the CTA's label tile and
-// "component size >= min" flags, (r, c) the pixel's tile coordinates.
-template <typename Emit>
-__device__ __forceinline__ void pixel_points(const uint32_t (*lab)[BP_SW], const uint8_t (*big)[BP_SW], int r, int c,
-                                             uint32_t x, uint32_t y, Emit emit) {
-    const uint32_t p = lab[r][c];
-    const uint32_t cp = p & LABEL_PIXEL_MASK, lp = p & LABEL_VALUE_MASK;
-    const bool bp = big[r][c];
-    auto test = [&](int t, int rr, int cc) {
-        uint32_t q = lab[rr][cc];
-        uint32_t cq = q & LABEL_PIXEL_MASK;
-        if (cq == cp) return;
-        if (!bp || !big[rr][cc]) return;
-        uint32_t lq = q & LABEL_VALUE_MASK;
-        uint32_t px = x | ((uint32_t)t << 14);
-        uint32_t py = cq > cp ? (COLOR_DIR_MASK | y) : y;
-        unsigned long long lo = min(lp, lq), hi = max(lp, lq);
-        emit((lo << 32) | hi, px | (py << 16));
-    };
-    test(0, r, c + 1);
-    {
-        uint32_t left = lab[r][c - 1], down = lab[r + 1][c];
-        bool dup = (left & LABEL_PIXEL_MASK) != (down & LABEL_PIXEL_MASK) && big[r][c - 1] && big[r + 1][c];
-        if (!dup) test(1, r + 1, c - 1);
-    }
-    test(2, r + 1, c);
-    test(3, r + 1, c + 1);
+// A staged point: CTA table slot (8 bits), tile-relative x (6) and y (4),
+// neighbour test (2) and colour direction (1).
+constexpr int BP_STAGE = BP_W * BP_H * 4;  // at most 4 points per pixel
+__device__ __forceinline__ uint32_t stage_entry(int ls, int xo, int yo, int t, int dir) {
+    return ((uint32_t)ls << 13) | (uint32_t)xo | ((uint32_t)yo << 6) | ((uint32_t)t << 10) | ((uint32_t)dir << 12);
+}
+__device__ __forceinline__ uint32_t stage_packed(uint32_t e, uint32_t x0, uint32_t y0) {
+    uint32_t x = x0 + (e & 63), y = y0 + ((e >> 6) & 15), t = (e >> 10) & 3, dir = (e >> 12) & 1;
+    return (x | (t << 14)) | ((y | (dir << 15)) << 16);
 }
 
+// find_boundaries (find_boundaries.cpp:10-155) fused with the per-pair
+// ClusterBounds reduction (main.cpp:571-585) and the compaction of points.
 __global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_constant__ FrameSet fs,
                                                                  uint32_t min_size) {
     const FrameDesc& F = fs.get(blockIdx.y);
@@ -202,8 +140,9 @@ __global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_co
     __shared__ uint32_t lab[BP_SH][BP_SW];
     __shared__ uint8_t big[BP_SH][BP_SW];
     __shared__ PairTableSmem T;
+    __shared__ uint32_t stage[BP_STAGE];
     __shared__ uint32_t red[33];
-    __shared__ uint32_t s_base;
+    __shared__ uint32_t s_nst, s_base;
 
     for (int i = threadIdx.x; i < BP_SH * BP_SW; i += blockDim.x) {
         int r = i / BP_SW, c = i % BP_SW;
@@ -217,85 +156,142 @@ __global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_co
         T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
         T.gx[i] = 0; T.gy[i] = 0; T.pxgx[i] = 0; T.gslot[i] = INVALID;
     }
+    if (threadIdx.x == 0) s_nst = 0;
     __syncthreads();
 
-    const int r = threadIdx.x / (BP_W / 4), c0 = (threadIdx.x % (BP_W / 4)) * 4;
-    const uint32_t y = y0 + r;
-    // pass 1: count and aggregate
-    Agg a0, a1;
-    agg_init(a0, EMPTY_KEY);
-    agg_init(a1, EMPTY_KEY);
-    uint32_t npts = 0;
-    if ((int)y < h) {
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            uint32_t x = x0 + c0 + k;
-            if (x == 0 || (int)x >= w) continue;
-            pixel_points(lab, big, r, c0 + k + 1, x, y, [&](unsigned long long key, uint32_t packed) {
-                npts++;
-                if (a0.key == key) { agg_add(a0, packed); return; }
-                if (a1.key == key) { agg_add(a1, packed); return; }
-                if (a0.key == EMPTY_KEY) { agg_init(a0, key); agg_add(a0, packed); return; }
-                if (a1.key != EMPTY_KEY) flush_agg(F, T, a1, status);
-                agg_init(a1, key);
-                agg_add(a1, packed);
-            });
+    // A: enumerate points in the reference's test order (R, BL unless it
+    // would duplicate, B, BR: find_boundaries.cpp:128-150), key them into
+    // the CTA table and stage them.
+    const int lane = threadIdx.x & 31;
+    const int r = threadIdx.x / (BP_W / 4), cbase = (threadIdx.x % (BP_W / 4)) * 4;
+    const int y = y0 + r;
+    unsigned long long last_key = EMPTY_KEY;
+    int last_ls = -1;
+#pragma unroll 1
+    for (int k = 0; k < 4; k++) {
+        const int xo = cbase + k, x = x0 + xo, c = xo + 1;
+        const bool pix_ok = y < h && x > 0 && x < w;
+        const uint32_t p = lab[r][c];
+        const uint32_t cp = p & LABEL_PIXEL_MASK, lp = p & LABEL_VALUE_MASK;
+        const bool bp = big[r][c];
+        const bool dup = (lab[r][c - 1] & LABEL_PIXEL_MASK) != (lab[r + 1][c] & LABEL_PIXEL_MASK) &&
+                         big[r][c - 1] && big[r + 1][c];
+#pragma unroll 1
+        for (int t = 0; t < 4; t++) {
+            const int rr = r + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
+            const uint32_t q = lab[rr][cc];
+            const uint32_t cq = q & LABEL_PIXEL_MASK;
+            const bool emit = pix_ok && bp && cq != cp && big[rr][cc] && !(t == 1 && dup);
+            int ls = 0;
+            if (emit) {
+                const uint32_t lq = q & LABEL_VALUE_MASK;
+                const unsigned long long key = ((unsigned long long)min(lp, lq) << 32) | max(lp, lq);
+                // consecutive points of a thread mostly share their pair
+                if (key == last_key) {
+                    ls = last_ls;
+                } else {
+                    ls = local_insert(T, key);
+                    last_key = key;
+                    last_ls = ls;
+                }
+                if (ls < 0) {  // CTA table full: account for and list the point directly
+                    uint32_t gs = global_insert(F, key);
+                    uint32_t xd = 2u * (uint32_t)x + 1u, yd = 2u * (uint32_t)y;
+                    int gx = cq > cp ? 1 : -1;
+                    atomicAdd(F.counters + CNT_ALLPOINTS, 1u);
+                    if (gs == INVALID) {
+                        atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
+                    } else {
+                        global_flush(F, gs, 1, xd, xd, yd, yd, gx, 0, (unsigned long long)(long long)((int)xd * gx));
+                        uint32_t pos = atomicAdd(F.counters + CNT_POINTS, 1u);
+                        uint32_t packed = ((uint32_t)x | ((uint32_t)t << 14)) |
+                                          (((uint32_t)y | (cq > cp ? 0x8000u : 0u)) << 16);
+                        if (pos < F.point_cap) F.points[pos] = ((unsigned long long)gs << 32) | packed;
+                        else atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
+                    }
+                }
+            }
+            const bool st = emit && ls >= 0;
+            const unsigned m = __ballot_sync(0xffffffffu, st);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                uint32_t b = 0;
+                if (lane == leader) b = atomicAdd(&s_nst, (uint32_t)__popc(m));
+                b = __shfl_sync(0xffffffffu, b, leader);
+                if (st) stage[b + __popc(m & ((1u << lane) - 1u))] = stage_entry(ls, xo, r, t, cq > cp ? 1 : 0);
+            }
         }
     }
-    // warp-level combine of the two running aggregates, then one set of
-    // shared-memory atomics per distinct key per warp
-#pragma unroll
-    for (int s = 0; s < 2; s++) {
-        Agg& a = s == 0 ? a0 : a1;
-        unsigned mask = __match_any_sync(0xffffffffu, a.key);
-        Agg b = a;
-        b.cnt = __reduce_add_sync(mask, a.cnt);
-        b.xmin = __reduce_min_sync(mask, a.xmin);
-        b.xmax = __reduce_max_sync(mask, a.xmax);
-        b.ymin = __reduce_min_sync(mask, a.ymin);
-        b.ymax = __reduce_max_sync(mask, a.ymax);
-        b.gx = __reduce_add_sync(mask, a.gx);
-        b.gy = __reduce_add_sync(mask, a.gy);
-        b.pxgx = __reduce_add_sync(mask, a.pxgx);
-        int leader = __ffs(mask) - 1;
-        if ((int)(threadIdx.x & 31) == leader && a.key != EMPTY_KEY) flush_agg(F, T, b, status);
+    __syncthreads();
+    const uint32_t nst = s_nst;
+
+    // B: per-pair sums of the staged points (warp groups by table slot)
+    for (uint32_t b0 = (threadIdx.x & ~31u); b0 < nst; b0 += blockDim.x) {
+        const uint32_t i = b0 + lane;
+        const bool v = i < nst;
+        const uint32_t e = v ? stage[i] : 0u;
+        const uint32_t ls = v ? (e >> 13) : 0xFFFFu;
+        const uint32_t xd = 2u * (uint32_t)(x0 + (e & 63)) + 1u, yd = 2u * (uint32_t)(y0 + ((e >> 6) & 15));
+        const int gx = ((e >> 12) & 1) ? 1 : -1;
+        const unsigned m = __match_any_sync(0xffffffffu, ls);
+        const uint32_t cnt = __reduce_add_sync(m, v ? 1u : 0u);
+        const uint32_t xmn = __reduce_min_sync(m, xd), xmx = __reduce_max_sync(m, xd);
+        const uint32_t ymn = __reduce_min_sync(m, yd), ymx = __reduce_max_sync(m, yd);
+        const int sgx = __reduce_add_sync(m, v ? gx : 0);
+        const int spx = __reduce_add_sync(m, v ? (int)xd * gx : 0);
+        if (v && lane == __ffs(m) - 1) {
+            atomicAdd(&T.cnt[ls], cnt);
+            atomicMin(&T.xmin[ls], xmn);
+            atomicMax(&T.xmax[ls], xmx);
+            atomicMin(&T.ymin[ls], ymn);
+            atomicMax(&T.ymax[ls], ymx);
+            atomicAdd(&T.gx[ls], sgx);
+            atomicAdd(&T.pxgx[ls], (unsigned long long)(long long)spx);
+        }
     }
     __syncthreads();
-    // merge the CTA's pairs into the frame's table
+
+    // C: merge into the frame's table.  A pair whose running point count
+    // already exceeds ValidBlobFilter's maximum 2 (2w + 2h)
+    // (cluster_bounds.h:92-93,102) can never survive; its points are counted
+    // but not listed.
+    const uint32_t max_pixels = 2u * (2u * (uint32_t)w + 2u * (uint32_t)h);
     for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
         unsigned long long key = T.key[i];
         if (key == EMPTY_KEY) continue;
         uint32_t gs = global_insert(F, key);
-        T.gslot[i] = gs;
         if (gs == INVALID) {
             atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
+            T.gslot[i] = INVALID;
             continue;
         }
-        global_flush(F, gs, T.cnt[i], T.xmin[i], T.xmax[i], T.ymin[i], T.ymax[i], T.gx[i], T.gy[i], T.pxgx[i]);
+        uint32_t old = global_flush(F, gs, T.cnt[i], T.xmin[i], T.xmax[i], T.ymin[i], T.ymax[i], T.gx[i], T.gy[i],
+                                    T.pxgx[i]);
+        T.gslot[i] = (old + T.cnt[i] > max_pixels) ? INVALID : gs;
     }
-    // reserve space in the point list
+    __syncthreads();
+
+    // D: list the points of live pairs (contiguous chunk per thread)
+    const uint32_t per = (nst + blockDim.x - 1) / blockDim.x;
+    const uint32_t i0 = min(nst, threadIdx.x * per), i1 = min(nst, i0 + per);
+    uint32_t nlive = 0;
+    for (uint32_t i = i0; i < i1; i++) nlive += T.gslot[stage[i] >> 13] != INVALID;
     uint32_t total;
-    uint32_t off = block_exclusive_scan_u32(npts, red, &total);
+    const uint32_t off = block_exclusive_scan_u32(nlive, red, &total);
     if (threadIdx.x == 0) {
         uint32_t b = total ? atomicAdd(F.counters + CNT_POINTS, total) : 0u;
+        if (nst) atomicAdd(F.counters + CNT_ALLPOINTS, nst);
         if ((unsigned long long)b + total > F.point_cap) atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
         s_base = b;
     }
     __syncthreads();
-    // pass 2: write the points tagged with their pair slot
-    if (npts) {
-        uint32_t pos = s_base + off;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            uint32_t x = x0 + c0 + k;
-            if (x == 0 || (int)x >= w) continue;
-            pixel_points(lab, big, r, c0 + k + 1, x, y, [&](unsigned long long key, uint32_t packed) {
-                int ls = local_lookup(T, key);
-                uint32_t gs = ls >= 0 ? T.gslot[ls] : global_lookup(F, key);
-                if (pos < F.point_cap) F.points[pos] = ((unsigned long long)gs << 32) | packed;
-                pos++;
-            });
-        }
+    uint32_t pos = s_base + off;
+    for (uint32_t i = i0; i < i1; i++) {
+        const uint32_t e = stage[i];
+        const uint32_t gs = T.gslot[e >> 13];
+        if (gs == INVALID) continue;
+        if (pos < F.point_cap) F.points[pos] = ((unsigned long long)gs << 32) | stage_packed(e, x0, y0);
+        pos++;
     }
 }
 
@@ -333,7 +329,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
     fp.tag_width = p.tag_width;
     fp.normal_border = p.normal_border;
     fp.reversed_border = p.reversed_border;
-    uint32_t carry_start = 0, carry_cluster = 0, carry_fstart = 0;
+    uint32_t carry_start = 0, carry_cluster = 0, carry_fstart = 0, carry_small = 0, carry_large = 0;
     for (uint32_t c0 = 0; c0 < C; c0 += blockDim.x) {
         uint32_t c = c0 + threadIdx.x;
         uint32_t slot = INVALID, cnt = 0;
@@ -349,12 +345,16 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
             pxgx = (long long)F.pair_pxgx[slot];
             keep = valid_blob(fp, cnt, bb.x, bb.y, bb.z, bb.w, gs.x, gs.y, pxgx);
         }
-        uint32_t tot_cnt, tot_keep, tot_fcnt;
+        uint32_t tot_cnt, tot_keep, tot_fcnt, tot_small, tot_large;
         uint32_t start = carry_start + block_exclusive_scan_u32(cnt, red, &tot_cnt);
         uint32_t cid = carry_cluster + block_exclusive_scan_u32(keep ? 1u : 0u, red, &tot_keep);
         uint32_t fstart = carry_fstart + block_exclusive_scan_u32(keep ? cnt : 0u, red, &tot_fcnt);
+        const bool fits = keep && cid < F.cluster_cap && (unsigned long long)fstart + cnt <= F.cpoint_cap;
+        const bool small = cnt <= CF_SMALL_CAP;
+        uint32_t js = carry_small + block_exclusive_scan_u32(fits && small ? 1u : 0u, red, &tot_small);
+        uint32_t jl = carry_large + block_exclusive_scan_u32(fits && !small ? 1u : 0u, red, &tot_large);
+        if (fits) F.cluster_work[small ? js : F.cluster_cap - 1 - jl] = cid;
         if (keep) {
-            bool fits = cid < F.cluster_cap && (unsigned long long)fstart + cnt <= F.cpoint_cap;
             if (!fits) {
                 atomicOr(status, ATAG_DEVFLAG_CLUSTER_OVERFLOW);
             } else {
@@ -377,39 +377,48 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
         carry_start += tot_cnt;
         carry_cluster += tot_keep;
         carry_fstart += tot_fcnt;
+        carry_small += tot_small;
+        carry_large += tot_large;
     }
     if (threadIdx.x == 0) {
         uint32_t ncl = carry_cluster, npf = carry_fstart;
         if (ncl > F.cluster_cap) ncl = F.cluster_cap;
         // clusters are assigned in order, so the kept prefix is [0, ncl)
-        uint32_t np = F.counters[CNT_POINTS];
         F.counters[CNT_CLUSTERS] = ncl;
+        F.counters[CNT_SMALL] = carry_small;
+        F.counters[CNT_LARGE] = carry_large;
         F.stats->width = F.width;
         F.stats->height = F.height;
-        F.stats->n_points = np < F.point_cap ? np : F.point_cap;
+        F.stats->n_points = F.counters[CNT_ALLPOINTS];
         F.stats->n_pairs = C;
         F.stats->n_clusters = ncl;
         F.stats->n_cluster_points = npf < F.cpoint_cap ? npf : F.cpoint_cap;
     }
 }
 
-// Prefix offsets of a per-frame count over the batch (flattened work space
-// for the per-cluster kernels) and reset of the work-queue cursor.
-__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, uint32_t which,
-                                uint32_t* __restrict__ offsets, uint32_t* __restrict__ work_counter) {
+// Prefix offsets of per-frame counts over the batch (the flattened work
+// spaces of the per-cluster kernels) and reset of their queue cursors.
+__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, uint32_t which0,
+                                uint32_t* __restrict__ offsets0, uint32_t which1, uint32_t* __restrict__ offsets1,
+                                uint32_t* __restrict__ work_counters) {
     __shared__ uint32_t red[33];
-    uint32_t carry = 0;
-    for (uint32_t f0 = 0; f0 < n_frames; f0 += blockDim.x) {
-        uint32_t f = f0 + threadIdx.x;
-        uint32_t v = f < n_frames ? fs.get(f).counters[which] : 0u;
-        uint32_t tot;
-        uint32_t e = block_exclusive_scan_u32(v, red, &tot);
-        if (f < n_frames) offsets[f] = carry + e;
-        carry += tot;
-    }
-    if (threadIdx.x == 0) {
-        offsets[n_frames] = carry;
-        *work_counter = 0;
+    for (int k = 0; k < 2; k++) {
+        uint32_t which = k ? which1 : which0;
+        uint32_t* offsets = k ? offsets1 : offsets0;
+        if (!offsets) continue;
+        uint32_t carry = 0;
+        for (uint32_t f0 = 0; f0 < n_frames; f0 += blockDim.x) {
+            uint32_t f = f0 + threadIdx.x;
+            uint32_t v = f < n_frames ? fs.get(f).counters[which] : 0u;
+            uint32_t tot;
+            uint32_t e = block_exclusive_scan_u32(v, red, &tot);
+            if (f < n_frames) offsets[f] = carry + e;
+            carry += tot;
+        }
+        if (threadIdx.x == 0) {
+            offsets[n_frames] = carry;
+            work_counters[k] = 0;
+        }
     }
 }
 
@@ -449,7 +458,6 @@ __global__ void __launch_bounds__(256) k_scatter_points(const __grid_constant__ 
 // ---------------------------------------------------------------------------
 // 4. one cluster per CTA: sort, moments, scan, errors, filter, peaks
 // ---------------------------------------------------------------------------
-constexpr int CF_THREADS = 512;
 
 __device__ __forceinline__ long long shfl_up_ll(long long v, int o) {
     return (long long)__shfl_up_sync(0xffffffffu, (unsigned long long)v, o);
@@ -509,15 +517,16 @@ __device__ __forceinline__ uint32_t find_frame(const uint32_t* offsets, uint32_t
     return lo;
 }
 
-__global__ void __launch_bounds__(CF_THREADS, 1) k_cluster_fit(const __grid_constant__ FrameSet fs,
-                                                             const uint32_t* __restrict__ work_offsets,
-                                                             uint32_t n_frames, uint32_t* __restrict__ work_counter,
-                                                             uint32_t sort_cap) {
+template <bool LARGE>
+__device__ __forceinline__ void cluster_fit(const FrameSet& fs, const uint32_t* __restrict__ work_offsets,
+                                            uint32_t n_frames, uint32_t* __restrict__ work_counter) {
     extern __shared__ unsigned long long smem_keys[];
+    constexpr uint32_t sort_cap = LARGE ? CF_LARGE_CAP : CF_SMALL_CAP;
     __shared__ long long red_m[32][6];
     __shared__ unsigned long long red64[32];
     __shared__ uint32_t red32[33];
-    __shared__ uint32_t s_item;
+    __shared__ uint32_t s_item, s_ncand, s_flag;
+    uint32_t* hist = reinterpret_cast<uint32_t*>(smem_keys + 2 * sort_cap);
     const uint32_t total = work_offsets[n_frames];
     for (;;) {
         __syncthreads();
@@ -527,72 +536,90 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_cluster_fit(const __grid_cons
         if (item >= total) return;
         const uint32_t fidx = find_frame(work_offsets, n_frames, item);
         const FrameDesc& F = fs.get(fidx);
-        const uint32_t cid = item - work_offsets[fidx];
+        const uint32_t j = item - work_offsets[fidx];
+        const uint32_t cid = F.cluster_work[LARGE ? F.cluster_cap - 1 - j : j];
         const atag_cluster_extents ext = F.cluster_extents[cid];
         const uint32_t n = ext.count, start = ext.start;
         const bool in_smem = n <= sort_cap;
-        unsigned long long* keys = in_smem ? smem_keys : F.sortbuf + start;
+        unsigned long long* A = in_smem ? smem_keys : F.sortbuf + start;
         if (in_smem)
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) keys[i] = F.sortbuf[start + i];
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) A[i] = F.sortbuf[start + i];
         __syncthreads();
-        bitonic_sort_u64(keys, n);
+        // sort by (theta, packed point): the reference's (cluster, slope)
+        // order (main.cpp:737-750) with ties fixed by the point
+        unsigned long long* X = A;
+        if (LARGE && n > 1024) {
+            unsigned long long* Bb = in_smem ? smem_keys + sort_cap
+                                             : reinterpret_cast<unsigned long long*>(F.errbuf + 2ull * start);
+            X = block_radix_sort_u64(A, Bb, n, hist, red32, &s_flag);
+        } else {
+            bitonic_sort_u64(A, n);
+        }
         __syncthreads();
-        // cluster points, moments and their inclusive scan
-        const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
-        const uint32_t i0 = min(n, threadIdx.x * per), i1 = min(n, i0 + per);
-        Moment tot{0, 0, 0, 0, 0, 0};
-        for (uint32_t i = i0; i < i1; i++) {
-            unsigned long long k = keys[i];
-            uint32_t packed = (uint32_t)k;
+        // ClusterPoints out; the key slot is reused for the line-fit inputs
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+            const unsigned long long k = X[i];
+            const uint32_t packed = (uint32_t)k;
             atag_cluster_point cp;
             cp.packed_x = (uint16_t)packed;
             cp.packed_y = (uint16_t)(packed >> 16);
             cp.slope = float_from_order_key((uint32_t)(k >> 32));
             F.cluster_points[start + i] = cp;
-            tot = m_add(tot, initial_linefit(packed, F.width, F.height, F.grey));
+            X[i] = linefit_rxyw(packed, F.width, F.height, F.grey);
         }
-        Moment run = block_exclusive_scan_moment(tot, red_m);
-        for (uint32_t i = i0; i < i1; i++) {
-            run = m_add(run, initial_linefit((uint32_t)keys[i], F.width, F.height, F.grey));
-            store_moment(F.line_fit + start + i, run);
+        __syncthreads();
+        // segmented inclusive scan of the moments (main.cpp:796-801)
+        {
+            const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+            const uint32_t i0 = min(n, threadIdx.x * per), i1 = min(n, i0 + per);
+            Moment tot{0, 0, 0, 0, 0, 0};
+            for (uint32_t i = i0; i < i1; i++) tot = m_add(tot, moment_of(X[i]));
+            Moment run = block_exclusive_scan_moment(tot, red_m);
+            for (uint32_t i = i0; i < i1; i++) {
+                run = m_add(run, moment_of(X[i]));
+                store_moment(F.line_fit + start + i, run);
+            }
         }
         __syncthreads();
         // errors of the windows around each point, then the cyclic filter
-        float* err = in_smem ? reinterpret_cast<float*>(smem_keys) : F.errbuf + 2ull * start;
+        float* err = reinterpret_cast<float*>(X);
         float* flt = err + n;
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-            err[i] = window_error(F.line_fit, start, n, (long long)start + i);
+        const atag_line_fit_point* cpts = F.line_fit + start;
+        const uint32_t kwin = min(20u, n / 12);
+        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) err[i] = window_error_local(cpts, n, kwin, i);
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
             float acc = 0.0f;
 #pragma unroll
             for (int j = 0; j < 7; j++) {
-                uint32_t t = (i + n + j - 3) % n;
+                int t = (int)i + j - 3;
+                t = t < 0 ? t + (int)n : (t >= (int)n ? t - (int)n : t);
                 acc = __fadd_rn(acc, __fmul_rn(err[t], filter_tap(j)));
             }
             flt[i] = acc;
         }
+        if (threadIdx.x == 0) s_ncand = 0;
         __syncthreads();
-        // strict local maxima with error != 0 (D10); global point 0 never
-        uint32_t mycount = 0;
+        // strict local maxima with error != 0 (D10), global point 0 excluded,
+        // compacted as (error, ~index) keys into the now free error array
+        unsigned long long* cand = reinterpret_cast<unsigned long long*>(err);
         for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
             float cur = flt[i];
-            bool is_max = cur > flt[(i + n - 1) % n] && cur > flt[(i + 1) % n] && cur != 0.0f &&
-                          !(cid == 0 && i == 0);
-            mycount += is_max;
+            float prev = flt[i == 0 ? n - 1 : i - 1], next = flt[i + 1 == n ? 0 : i + 1];
+            if (cur > prev && cur > next && cur != 0.0f && !(cid == 0 && i == 0)) {
+                uint32_t pos = atomicAdd(&s_ncand, 1u);
+                cand[pos] = ((unsigned long long)float_order_key(cur) << 32) | (uint32_t)(~i);
+            }
         }
-        const uint32_t npeaks = block_sum_u32(mycount, red32);
+        __syncthreads();
+        const uint32_t npeaks = s_ncand;
         // the 10 best by (error desc, index asc): repeated block argmax
         unsigned long long last = ~0ull;
         const uint32_t take = npeaks < 10 ? npeaks : 10;
         for (uint32_t j = 0; j < take; j++) {
             unsigned long long best = 0;
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-                float cur = flt[i];
-                bool is_max = cur > flt[(i + n - 1) % n] && cur > flt[(i + 1) % n] && cur != 0.0f &&
-                              !(cid == 0 && i == 0);
-                if (!is_max) continue;
-                unsigned long long key = ((unsigned long long)float_order_key(cur) << 32) | (uint32_t)(~i);
+            for (uint32_t c = threadIdx.x; c < npeaks; c += blockDim.x) {
+                unsigned long long key = cand[c];
                 if (key < last && key > best) best = key;
             }
             best = block_max_u64(best, red64);
@@ -607,6 +634,19 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_cluster_fit(const __grid_cons
         }
         if (threadIdx.x == 0) F.peak_count[cid] = npeaks;
     }
+}
+
+__global__ void __launch_bounds__(CF_SMALL_THREADS, 4) k_cluster_fit_small(const __grid_constant__ FrameSet fs,
+                                                                          const uint32_t* __restrict__ work_offsets,
+                                                                          uint32_t n_frames,
+                                                                          uint32_t* __restrict__ work_counter) {
+    cluster_fit<false>(fs, work_offsets, n_frames, work_counter);
+}
+__global__ void __launch_bounds__(CF_LARGE_THREADS, 1) k_cluster_fit_large(const __grid_constant__ FrameSet fs,
+                                                                          const uint32_t* __restrict__ work_offsets,
+                                                                          uint32_t n_frames,
+                                                                          uint32_t* __restrict__ work_counter) {
+    cluster_fit<true>(fs, work_offsets, n_frames, work_counter);
 }
 
 // ---------------------------------------------------------------------------

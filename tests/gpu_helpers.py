@@ -54,23 +54,39 @@ def oracle_top10(res):
     return counts, top
 
 
-def pair_point_set(views):
-    """GPU boundary points as a sorted array of (key, packed) from the pair
-    table, comparable with the oracle's (keys, points)."""
+def pair_table(views):
+    """Occupied slots of the GPU pair table as arrays sorted by key:
+    (key, count, x_min, x_max, y_min, y_max, gx_sum, gy_sum, pxgx)."""
+    keys = views["pair_keys"]
+    occ = np.flatnonzero(keys != np.uint64(0xFFFFFFFFFFFFFFFF))
+    occ = occ[np.argsort(keys[occ], kind="stable")]
+    bb, gs = views["pair_bbox"][occ], views["pair_gsum"][occ]
+    return (keys[occ], views["pair_count"][occ], bb[:, 0], bb[:, 1], bb[:, 2], bb[:, 3], gs[:, 0], gs[:, 1],
+            views["pair_pxgx"][occ])
+
+
+def oracle_pair_table(res):
+    b = res["bounds"]
+    return (res["bound_keys"], b["count"], b["x_min"], b["x_max"], b["y_min"], b["y_max"], b["gx_sum"],
+            b["gy_sum"], b["pxgx_pygy_sum"])
+
+
+def surviving_point_sets(views, res):
+    """(key, packed) of the points of the surviving clusters, sorted, from the
+    GPU's point list and from the oracle."""
     pp = views["pair_points"]
     slots = (pp >> np.uint64(32)).astype(np.int64)
     packed = (pp & np.uint64(0xFFFFFFFF)).astype(np.uint64)
     keys = views["pair_keys"][slots]
-    order = np.lexsort((packed, keys))
-    return keys[order], packed[order]
-
-
-def oracle_point_set(res):
+    keep = np.isin(keys, res["filtered_keys"])
+    gk, gp = keys[keep], packed[keep]
+    o = np.lexsort((gp, gk))
     p = res["points"]
-    packed = p["packed_x"].astype(np.uint64) | (p["packed_y"].astype(np.uint64) << np.uint64(16))
-    keys = res["keys"]
-    order = np.lexsort((packed, keys))
-    return keys[order], packed[order]
+    op = p["packed_x"].astype(np.uint64) | (p["packed_y"].astype(np.uint64) << np.uint64(16))
+    okeep = np.isin(res["keys"], res["filtered_keys"])
+    ok, op = res["keys"][okeep], op[okeep]
+    o2 = np.lexsort((op, ok))
+    return (gk[o], gp[o]), (ok[o2], op[o2])
 
 
 def assert_quads_match(gpu_q, ora_q, tol=CORNER_TOL_PX):
@@ -90,9 +106,12 @@ def assert_detect_matches(views, gpu_quads, res, cfg_compat=True):
     assert_same(views["labels"], res["labels"], "labels")
     assert_same(views["sizes"], res["sizes"], "sizes")
     assert int(st["n_points"]) == len(res["points"])
-    gk, gp = pair_point_set(views)
-    ok, op = oracle_point_set(res)
-    assert np.array_equal(gk, ok) and np.array_equal(gp, op)
+    for name, g, o in zip(("key", "count", "x_min", "x_max", "y_min", "y_max", "gx_sum", "gy_sum", "pxgx"),
+                          pair_table(views), oracle_pair_table(res)):
+        assert_same(np.asarray(g).astype(np.int64), np.asarray(o).astype(np.int64), f"pair {name}")
+    (gk, gp), (ok, op) = surviving_point_sets(views, res)
+    assert_same(gk, ok, "surviving point keys")
+    assert_same(gp, op, "surviving points")
     assert int(st["n_pairs"]) == len(res["bounds"])
     assert int(st["n_clusters"]) == len(res["filtered"])
     assert_same(views["cluster_keys"], res["filtered_keys"], "cluster_keys")

@@ -103,3 +103,16 @@ def test_host_buffer_path_matches(det1080, ref_images):
     res = oracle.detect(img)
     assert_quads_match(q_host, res["quads"])
     assert int(st["n_quads"]) == len(res["quads"])
+
+
+def test_detect_4k_stress():
+    """3840x2160 with 3000 clutter shapes and salt-and-pepper noise: many
+    pairs, clusters above the shared-memory sort capacity (global-memory
+    radix path) and deep union-find merges."""
+    from atag.detector import Detector
+    img = synth_frame("4k", 1)
+    det = Detector(3840, 2160)
+    quads, views = _run(det, img)
+    res = oracle.detect(img)
+    assert_detect_matches(views, quads, res)
+    assert int(res["extents"]["count"].max()) > 12288  # exercises the global-memory sort
