@@ -194,6 +194,18 @@ atag_status atag_image_segmentation(const uint8_t *d_thresholded, uint32_t *d_la
                                     uint32_t *d_labels, uint32_t *d_sizes, size_t sizes_elem,
                                     size_t width, size_t height, atag_stream_t stream);
 
+/* Same as atag_image_segmentation, for callers that must not allocate device
+ * memory (no counterpart in the reference).  The union-find forest lives in
+ * a 2,097,152-word array inside the library (8 MiB per GPU, held until the
+ * process exits) instead of a caller buffer; frames larger than 2,097,152
+ * pixels are rejected with ATAG_ERR_INVALID_ARGUMENT.  The first call on
+ * each device looks up that array's device address, so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller.  Allocates nothing. */
+atag_status atag_image_segmentation_noalloc(const uint8_t *d_thresholded, uint32_t *d_labels,
+                                            uint32_t *d_sizes, size_t width, size_t height,
+                                            atag_stream_t stream);
+
 /* Replaces find_boundaries (include/find_boundaries.h:8-12,
  * src/find_boundaries.cpp:10-155): the dense 4-plane output at
  * plane*w*h + y*w + x.  The caller pre-fills points with 0 and blob_labels

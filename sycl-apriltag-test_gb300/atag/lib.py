@@ -33,6 +33,7 @@ _SIGNATURES = {
     "atag_decimate": (_ST, [_P, _SZ, _SZ, _SZ, _P, _P]),
     "atag_threshold_image": (_ST, [_P, _P, _P, _P, _SZ, _SZ, _P]),
     "atag_image_segmentation": (_ST, [_P, _P, _P, _P, _SZ, _SZ, _SZ, _P]),
+    "atag_image_segmentation_noalloc": (_ST, [_P, _P, _P, _SZ, _SZ, _P]),
     "atag_find_boundaries": (_ST, [_P, _P, _P, _P, _SZ, _SZ, _P]),
     "atag_fit_lines": (_ST, [_P, _P, _P, _SZ, _P, _P]),
     "atag_do_indexing": (_ST, [_P, _SZ, _P, _P, _P, _P, _P]),

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "atag_internal.h"
 #include "atag_kernels.cuh"
 
 using namespace atag;
@@ -195,6 +196,11 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, FrameDe
 constexpr int RING = 16;
 
 }  // namespace
+
+namespace atag {
+atag_status set_error(atag_status s, const char* msg) { return fail(s, "%s", msg); }
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace atag
 
 // ===========================================================================
 // detector
