@@ -1036,6 +1036,41 @@ void oracle_free(oracle_result *r) {
     memset(r, 0, sizeof *r);
 }
 
+/* ------------------------------------------------------------------ */
+/* Batch evaluation of the record helpers (golden-vector checks).     */
+/* ------------------------------------------------------------------ */
+void oracle_eval_bounds(const atag_cluster_bounds *b, const atag_boundary_point *p, size_t n, size_t w,
+                        size_t h, float *cx, float *cy, float *theta, float *dot, uint8_t *valid) {
+    atag_config cfg;
+    oracle_config_default(&cfg);
+    for (size_t i = 0; i < n; i++) {
+        cx[i] = oracle_bounds_cx(&b[i]);
+        cy[i] = oracle_bounds_cy(&b[i]);
+        theta[i] = oracle_calc_theta(p[i], cx[i], cy[i]);
+        dot[i] = oracle_bounds_dot(&b[i]);
+        valid[i] = (uint8_t)oracle_valid_blob(&b[i], w, h, &cfg);
+    }
+}
+
+void oracle_eval_linefit(const atag_cluster_point *p, size_t n, uint32_t w, uint32_t h, const uint8_t *img,
+                         atag_line_fit_point *out) {
+    for (size_t i = 0; i < n; i++) out[i] = oracle_initial_linefit(p[i], w, h, img);
+}
+
+void oracle_eval_fit_line(const atag_line_fit_point *m, const uint64_t *nim, size_t n, float *lp, float *err,
+                          float *mse) {
+    for (size_t i = 0; i < n; i++) oracle_fit_line(&m[i], (size_t)nim[i], &lp[4 * i], &err[i], &mse[i]);
+}
+
+void oracle_eval_get_moment(const atag_line_fit_point *pre, size_t np, const uint64_t *ranges, size_t n,
+                            atag_line_fit_point *out, uint64_t *nout) {
+    for (size_t i = 0; i < n; i++) {
+        size_t c;
+        oracle_get_moment(pre, np, (size_t)ranges[2 * i], (size_t)ranges[2 * i + 1], &out[i], &c);
+        nout[i] = c;
+    }
+}
+
 int oracle_detect_many(const uint8_t *const *srcs, const int *src_w, const int *src_h, size_t n,
                        const atag_config *cfg, int threads, uint32_t *n_quads) {
     int used = 1;

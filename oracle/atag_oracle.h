@@ -107,6 +107,16 @@ int oracle_detect(const uint8_t *src, int src_w, int src_h, const atag_config *c
                   oracle_result *res);
 void oracle_free(oracle_result *res);
 
+/* Batch evaluation of the record helpers (golden-vector checks). */
+void oracle_eval_bounds(const atag_cluster_bounds *b, const atag_boundary_point *p, size_t n, size_t w,
+                        size_t h, float *cx, float *cy, float *theta, float *dot, uint8_t *valid);
+void oracle_eval_linefit(const atag_cluster_point *p, size_t n, uint32_t w, uint32_t h, const uint8_t *img,
+                         atag_line_fit_point *out);
+void oracle_eval_fit_line(const atag_line_fit_point *m, const uint64_t *nim, size_t n, float *lp, float *err,
+                          float *mse);
+void oracle_eval_get_moment(const atag_line_fit_point *pre, size_t np, const uint64_t *ranges, size_t n,
+                            atag_line_fit_point *out, uint64_t *nout);
+
 /* Throughput helper for the CPU baseline: runs oracle_detect on n frames
  * with up to `threads` OpenMP threads; writes each frame's quad count.
  * Returns the number of threads used. */

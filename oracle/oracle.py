@@ -88,6 +88,10 @@ def lib():
         L.oracle_hypotf.restype = ctypes.c_float
         L.oracle_hypotf.argtypes = [ctypes.c_float, ctypes.c_float]
         L.oracle_combination_decode.argtypes = [ctypes.c_uint32, _P]
+        L.oracle_eval_bounds.argtypes = [_P, _P, _SZ, _SZ, _SZ, _P, _P, _P, _P, _P]
+        L.oracle_eval_linefit.argtypes = [_P, _SZ, ctypes.c_uint32, ctypes.c_uint32, _P, _P]
+        L.oracle_eval_fit_line.argtypes = [_P, _P, _SZ, _P, _P, _P]
+        L.oracle_eval_get_moment.argtypes = [_P, _SZ, _P, _SZ, _P, _P]
         L.oracle_detect_many.restype = ctypes.c_int
         L.oracle_detect_many.argtypes = [_P, _P, _P, _SZ, ctypes.POINTER(Config), ctypes.c_int, _P]
         _lib = L
@@ -246,3 +250,43 @@ def detect_many(frames, cfg: Config = None, threads: int = 0):
     used = lib().oracle_detect_many(ctypes.cast(ptrs, ctypes.c_void_p), _ptr(ws), _ptr(hs), n,
                                     ctypes.byref(cfg), threads, _ptr(nq))
     return nq, used
+
+
+def eval_bounds(bounds, points, width, height):
+    """cx, cy, calc_theta(cx, cy), dot and ValidBlobFilter for each record."""
+    b = np.ascontiguousarray(bounds)
+    p = np.ascontiguousarray(points)
+    n = len(b)
+    cx, cy, th, dot = (np.zeros(n, np.float32) for _ in range(4))
+    valid = np.zeros(n, np.uint8)
+    lib().oracle_eval_bounds(_ptr(b), _ptr(p), n, width, height, _ptr(cx), _ptr(cy), _ptr(th), _ptr(dot),
+                             _ptr(valid))
+    return cx, cy, th, dot, valid
+
+
+def eval_linefit(cluster_points, width, height, image):
+    cp = np.ascontiguousarray(cluster_points)
+    img = np.ascontiguousarray(image, dtype=np.uint8)
+    out = np.zeros(len(cp), LINE_FIT_POINT)
+    lib().oracle_eval_linefit(_ptr(cp), len(cp), width, height, _ptr(img), _ptr(out))
+    return out
+
+
+def eval_fit_line(moments, num_in_moment):
+    m = np.ascontiguousarray(moments)
+    nim = np.ascontiguousarray(num_in_moment, dtype=np.uint64)
+    n = len(m)
+    lp = np.zeros(4 * n, np.float32)
+    err, mse = np.zeros(n, np.float32), np.zeros(n, np.float32)
+    lib().oracle_eval_fit_line(_ptr(m), _ptr(nim), n, _ptr(lp), _ptr(err), _ptr(mse))
+    return lp, err, mse
+
+
+def eval_get_moment(prefix, ranges):
+    pre = np.ascontiguousarray(prefix)
+    r = np.ascontiguousarray(ranges, dtype=np.uint64)
+    n = len(r) // 2
+    out = np.zeros(n, LINE_FIT_POINT)
+    cnt = np.zeros(n, np.uint64)
+    lib().oracle_eval_get_moment(_ptr(pre), len(pre), _ptr(r), n, _ptr(out), _ptr(cnt))
+    return out, cnt

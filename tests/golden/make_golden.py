@@ -1,0 +1,95 @@
+"""Generates the golden vectors under tests/golden from the reference's own
+sources.  Run in a tree where the reference is mounted (it builds
+oracle/_ref/refshim_harness from the reference's src/threshold.cpp,
+src/segmentation.cpp, src/find_boundaries.cpp, src/fit_quad.cpp and
+include/*.h; see oracle/refshim/).
+
+Writes:
+  reference_images.npz  the reference's three input PNGs, decoded
+  small_frames.npz      small hand-made and synthetic frames
+  records.npz           record helpers (Combinadics decode, calc_theta,
+                        ClusterBounds::cx/cy/dot, ValidBlobFilter,
+                        compute_initial_linefit, fit_line, get_moment) on
+                        seeded inputs
+  pipeline.json         per frame and per stage: element count and SHA-256 of
+                        the canonical bytes (record padding excluded)
+"""
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "sycl-apriltag-test_gb300"))
+
+import golden_io  # noqa: E402
+
+REF = os.environ.get("ATAG_REFERENCE_TREE", "/root/reference")
+
+
+def small_frames():
+    from atag import synth
+    rng = np.random.default_rng(7)
+    out = {
+        "noise_64": rng.integers(0, 256, (64, 64), dtype=np.uint8),
+        "noise_68x132": rng.integers(0, 256, (68, 132), dtype=np.uint8),
+        "checker_96x128": ((np.indices((96, 128)).sum(0) // 8) % 2 * 255).astype(np.uint8),
+        "flat_32": np.full((32, 32), 100, np.uint8),
+        "tiny_4x4": rng.integers(0, 256, (4, 4), dtype=np.uint8),
+    }
+    b = rng.integers(0, 2, (20, 28)).astype(np.uint8) * 255
+    out["blocky_80x112"] = np.kron(b, np.ones((4, 4), np.uint8))
+    sq = np.full((120, 160), 230, np.uint8)
+    sq[30:90, 50:110] = 20
+    sq[45:75, 65:95] = 230
+    out["square_120x160"] = sq
+    for seed in (1, 2, 3):
+        img = synth.render(synth.CONFIGS["vga"], seed)
+        out[f"vga_seed{seed}_d2"] = np.ascontiguousarray(img[::2, ::2])
+    return out
+
+
+def run_pipeline(harness, img, tmp):
+    img.tofile(os.path.join(tmp, "in.raw"))
+    subprocess.run([harness, os.path.join(tmp, "in.raw"), str(img.shape[1]), str(img.shape[0]), tmp], check=True,
+                   capture_output=True)
+    out = {}
+    for name, dtype in golden_io.PIPELINE_ARRAYS.items():
+        a = np.fromfile(os.path.join(tmp, name + ".bin"), dtype=dtype)
+        out[name] = {"n": int(len(a)), "sha256": golden_io.digest(a)}
+    return out
+
+
+def main():
+    sys.path.insert(0, os.path.join(ROOT, "oracle", "refshim"))
+    import build_refshim
+    harness = build_refshim.build()
+    if harness is None:
+        raise SystemExit(f"reference tree not found at {REF}")
+    from pngdecode import read_png_grey
+    imgs = {n[:-4]: read_png_grey(os.path.join(REF, n)) for n in ("decimate.png", "decimate4.png", "decimate2.png")}
+    np.savez_compressed(os.path.join(HERE, "reference_images.npz"), **imgs)
+    small = small_frames()
+    np.savez_compressed(os.path.join(HERE, "small_frames.npz"), **small)
+    pipeline = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, img in list(imgs.items()) + list(small.items()):
+            pipeline[name] = run_pipeline(harness, img, tmp)
+        subprocess.run([harness, "--records", tmp], check=True, capture_output=True)
+        rec = {name: np.fromfile(os.path.join(tmp, name + ".bin"), dtype=dt)
+               for name, dt in golden_io.RECORD_ARRAYS.items()}
+    np.savez_compressed(os.path.join(HERE, "records.npz"), **rec)
+    with open(os.path.join(HERE, "pipeline.json"), "w") as f:
+        json.dump(pipeline, f, indent=1, sort_keys=True)
+    print("golden vectors written:", ", ".join(sorted(pipeline)))
+
+
+if __name__ == "__main__":
+    main()
