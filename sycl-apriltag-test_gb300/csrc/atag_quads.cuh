@@ -92,6 +92,83 @@ __device__ __forceinline__ int choose_combination(float err, uint32_t n, unsigne
     return chosen == 0xFFFFFFFFu ? -1 : (int)chosen;
 }
 
+// do_indexing for one peak cluster on a 256-thread CTA.  The 210
+// combinations of up to 10 peaks only ever fit the 90 ordered segments
+// between two of those peaks, so each segment is fitted once (the same
+// get_moment/fit_line calls as the per-combination form, hence the same
+// bits) and every combination sums four table entries in the reference's
+// order (fit_quad.cpp:445-498).  Writes *out only when a combination is
+// chosen; returns the chosen number or -1.
+struct SegmentTable {
+    float err[10][10], mse[10][10], lp[10][10][4];
+    Moment m[10][10];
+    uint16_t nim[10][10];
+    uint32_t idx[10];        // line_fit_point_index of peak rank r
+};
+
+__device__ __forceinline__ int index_one_cluster(uint32_t count, const atag_corner* __restrict__ corners,
+                                                 const atag_line_fit_point* __restrict__ cpts, uint32_t ccount,
+                                                 float max_mse, float cos_critical, SegmentTable& T,
+                                                 uint32_t* red32, atag_fitted_quad* out) {
+    const uint32_t m = count < 10u ? count : 10u;
+    const uint32_t ncomb = n_choose_4(m);
+    if (ncomb == 0) return -1;
+    if (threadIdx.x < m) T.idx[threadIdx.x] = corners[threadIdx.x].line_fit_point_index;
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < m * m; s += blockDim.x) {
+        const uint32_t a = s / m, b = s % m;
+        if (a == b) continue;
+        const unsigned long long i0 = T.idx[a], i1 = T.idx[b];
+        unsigned long long nim;
+        Moment mo = get_moment(cpts, ccount, i0, i1, &nim);
+        float e, mse;
+        fit_line(mo, nim, i0 < i1 ? T.lp[a][b] : nullptr, &e, &mse);
+        T.err[a][b] = e;
+        T.mse[a][b] = mse;
+        T.m[a][b] = mo;
+        T.nim[a][b] = (uint16_t)nim;
+    }
+    __syncthreads();
+    const uint32_t n = threadIdx.x;
+    float err = __int_as_float(0x7f800000);
+    uint32_t r[4] = {0, 0, 0, 0};
+    if (n < ncomb) {
+        uint32_t d[4];
+        combination_decode(n, d);
+        // sort_4 on the line-fit indices (fit_quad.cpp:437), tracking ranks
+        unsigned long long v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) v[j] = ((unsigned long long)T.idx[d[j]] << 8) | d[j];
+        sort_4(v);
+#pragma unroll
+        for (int j = 0; j < 4; j++) r[j] = (uint32_t)(v[j] & 0xFF);
+        float total = 0.0f;
+        bool valid = true;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t a = r[j], b = r[(j + 1) & 3];
+            valid &= T.mse[a][b] <= max_mse;
+            total = __fadd_rn(total, T.err[a][b]);
+        }
+        const float* p01 = T.lp[r[0]][r[1]];
+        const float* p12 = T.lp[r[1]][r[2]];
+        float dot = __fadd_rn(__fmul_rn(p01[2], p12[2]), __fmul_rn(p01[3], p12[3]));
+        valid &= fabsf(dot) <= cos_critical;
+        if (valid && !isnan(total)) err = total;
+    }
+    const int chosen = choose_combination(err, n, nullptr, red32);
+    if (chosen >= 0 && (int)n == chosen) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t a = r[j], b = r[(j + 1) & 3];
+            store_moment(&out->moments[j], T.m[a][b]);
+            out->num_in_moments[j] = T.nim[a][b];
+            out->indices[j] = (uint16_t)T.idx[a];
+        }
+    }
+    return chosen;
+}
+
 __device__ __forceinline__ void write_fitted(atag_fitted_quad* out, const Combination& c) {
 #pragma unroll
     for (int s = 0; s < 4; s++) store_moment(&out->moments[s], c.m[s]);

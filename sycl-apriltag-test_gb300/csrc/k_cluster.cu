@@ -118,6 +118,7 @@ __device__ __forceinline__ uint32_t global_flush(const FrameDesc& F, uint32_t gs
 // A staged point: CTA table slot (8 bits), tile-relative x (6) and y (4),
 // neighbour test (2) and colour direction (1).
 constexpr int BP_STAGE = BP_W * BP_H * 4;  // at most 4 points per pixel
+constexpr uint32_t STAGE_DIRECT = 1u << 21; // point already accounted for in global memory
 __device__ __forceinline__ uint32_t stage_entry(int ls, int xo, int yo, int t, int dir) {
     return ((uint32_t)ls << 13) | (uint32_t)xo | ((uint32_t)yo << 6) | ((uint32_t)t << 10) | ((uint32_t)dir << 12);
 }
@@ -142,7 +143,7 @@ __global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_co
     __shared__ PairTableSmem T;
     __shared__ uint32_t stage[BP_STAGE];
     __shared__ uint32_t red[33];
-    __shared__ uint32_t s_nst, s_base;
+    __shared__ uint32_t s_base;
 
     for (int i = threadIdx.x; i < BP_SH * BP_SW; i += blockDim.x) {
         int r = i / BP_SW, c = i % BP_SW;
@@ -156,81 +157,79 @@ __global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_co
         T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
         T.gx[i] = 0; T.gy[i] = 0; T.pxgx[i] = 0; T.gslot[i] = INVALID;
     }
-    if (threadIdx.x == 0) s_nst = 0;
     __syncthreads();
 
     // A: enumerate points in the reference's test order (R, BL unless it
-    // would duplicate, B, BR: find_boundaries.cpp:128-150), key them into
-    // the CTA table and stage them.
+    // would duplicate, B, BR: find_boundaries.cpp:128-150).  First a 4-bit
+    // emission mask per pixel, then positions from one block scan, then the
+    // pair key of each emitted point goes into the CTA table and the point
+    // into the staging list.
     const int lane = threadIdx.x & 31;
     const int r = threadIdx.x / (BP_W / 4), cbase = (threadIdx.x % (BP_W / 4)) * 4;
     const int y = y0 + r;
-    unsigned long long last_key = EMPTY_KEY;
-    int last_ls = -1;
-#pragma unroll 1
+    uint32_t masks = 0;
+#pragma unroll
     for (int k = 0; k < 4; k++) {
         const int xo = cbase + k, x = x0 + xo, c = xo + 1;
-        const bool pix_ok = y < h && x > 0 && x < w;
-        const uint32_t p = lab[r][c];
-        const uint32_t cp = p & LABEL_PIXEL_MASK, lp = p & LABEL_VALUE_MASK;
-        const bool bp = big[r][c];
+        if (!(y < h && x > 0 && x < w) || !big[r][c]) continue;
+        const uint32_t cp = lab[r][c] & LABEL_PIXEL_MASK;
         const bool dup = (lab[r][c - 1] & LABEL_PIXEL_MASK) != (lab[r + 1][c] & LABEL_PIXEL_MASK) &&
                          big[r][c - 1] && big[r + 1][c];
-#pragma unroll 1
-        for (int t = 0; t < 4; t++) {
+        uint32_t m = 0;
+        m |= ((lab[r][c + 1] & LABEL_PIXEL_MASK) != cp && big[r][c + 1]) ? 1u : 0u;
+        m |= (!dup && (lab[r + 1][c - 1] & LABEL_PIXEL_MASK) != cp && big[r + 1][c - 1]) ? 2u : 0u;
+        m |= ((lab[r + 1][c] & LABEL_PIXEL_MASK) != cp && big[r + 1][c]) ? 4u : 0u;
+        m |= ((lab[r + 1][c + 1] & LABEL_PIXEL_MASK) != cp && big[r + 1][c + 1]) ? 8u : 0u;
+        masks |= m << (4 * k);
+    }
+    uint32_t nst;
+    uint32_t pos = block_exclusive_scan_u32((uint32_t)__popc(masks), red, &nst);
+    if (masks) {
+        unsigned long long last_key = EMPTY_KEY;
+        int last_ls = -1;
+        for (uint32_t mm = masks; mm; mm &= mm - 1) {
+            const int bit = __ffs(mm) - 1, k = bit >> 2, t = bit & 3;
+            const int xo = cbase + k, x = x0 + xo, c = xo + 1;
             const int rr = r + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
-            const uint32_t q = lab[rr][cc];
-            const uint32_t cq = q & LABEL_PIXEL_MASK;
-            const bool emit = pix_ok && bp && cq != cp && big[rr][cc] && !(t == 1 && dup);
-            int ls = 0;
-            if (emit) {
-                const uint32_t lq = q & LABEL_VALUE_MASK;
-                const unsigned long long key = ((unsigned long long)min(lp, lq) << 32) | max(lp, lq);
-                // consecutive points of a thread mostly share their pair
-                if (key == last_key) {
-                    ls = last_ls;
+            const uint32_t p = lab[r][c], q = lab[rr][cc];
+            const uint32_t lp = p & LABEL_VALUE_MASK, lq = q & LABEL_VALUE_MASK;
+            const int dir = (q & LABEL_PIXEL_MASK) > (p & LABEL_PIXEL_MASK) ? 1 : 0;
+            const unsigned long long key = ((unsigned long long)min(lp, lq) << 32) | max(lp, lq);
+            int ls;
+            if (key == last_key) {  // consecutive points of a thread mostly share their pair
+                ls = last_ls;
+            } else {
+                ls = local_insert(T, key);
+                last_key = key;
+                last_ls = ls;
+            }
+            uint32_t e = stage_entry(ls < 0 ? 0 : ls, xo, r, t, dir);
+            if (ls < 0) {  // CTA table full: account for and list the point directly
+                e |= STAGE_DIRECT;
+                const uint32_t gs = global_insert(F, key);
+                const uint32_t xd = 2u * (uint32_t)x + 1u, yd = 2u * (uint32_t)y;
+                const int gx = dir ? 1 : -1;
+                if (gs == INVALID) {
+                    atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
                 } else {
-                    ls = local_insert(T, key);
-                    last_key = key;
-                    last_ls = ls;
-                }
-                if (ls < 0) {  // CTA table full: account for and list the point directly
-                    uint32_t gs = global_insert(F, key);
-                    uint32_t xd = 2u * (uint32_t)x + 1u, yd = 2u * (uint32_t)y;
-                    int gx = cq > cp ? 1 : -1;
-                    atomicAdd(F.counters + CNT_ALLPOINTS, 1u);
-                    if (gs == INVALID) {
-                        atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
-                    } else {
-                        global_flush(F, gs, 1, xd, xd, yd, yd, gx, 0, (unsigned long long)(long long)((int)xd * gx));
-                        uint32_t pos = atomicAdd(F.counters + CNT_POINTS, 1u);
-                        uint32_t packed = ((uint32_t)x | ((uint32_t)t << 14)) |
-                                          (((uint32_t)y | (cq > cp ? 0x8000u : 0u)) << 16);
-                        if (pos < F.point_cap) F.points[pos] = ((unsigned long long)gs << 32) | packed;
-                        else atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
-                    }
+                    global_flush(F, gs, 1, xd, xd, yd, yd, gx, 0, (unsigned long long)(long long)((int)xd * gx));
+                    const uint32_t at = atomicAdd(F.counters + CNT_POINTS, 1u);
+                    if (at < F.point_cap) F.points[at] = ((unsigned long long)gs << 32) | stage_packed(e, x0, y0);
+                    else atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
                 }
             }
-            const bool st = emit && ls >= 0;
-            const unsigned m = __ballot_sync(0xffffffffu, st);
-            if (m) {
-                const int leader = __ffs(m) - 1;
-                uint32_t b = 0;
-                if (lane == leader) b = atomicAdd(&s_nst, (uint32_t)__popc(m));
-                b = __shfl_sync(0xffffffffu, b, leader);
-                if (st) stage[b + __popc(m & ((1u << lane) - 1u))] = stage_entry(ls, xo, r, t, cq > cp ? 1 : 0);
-            }
+            stage[pos++] = e;
         }
     }
     __syncthreads();
-    const uint32_t nst = s_nst;
 
     // B: per-pair sums of the staged points (warp groups by table slot)
     for (uint32_t b0 = (threadIdx.x & ~31u); b0 < nst; b0 += blockDim.x) {
         const uint32_t i = b0 + lane;
-        const bool v = i < nst;
-        const uint32_t e = v ? stage[i] : 0u;
-        const uint32_t ls = v ? (e >> 13) : 0xFFFFu;
+        const uint32_t e0 = i < nst ? stage[i] : STAGE_DIRECT;
+        const bool v = !(e0 & STAGE_DIRECT);
+        const uint32_t e = v ? e0 : 0u;
+        const uint32_t ls = v ? ((e >> 13) & 255) : 0xFFFFu;
         const uint32_t xd = 2u * (uint32_t)(x0 + (e & 63)) + 1u, yd = 2u * (uint32_t)(y0 + ((e >> 6) & 15));
         const int gx = ((e >> 12) & 1) ? 1 : -1;
         const unsigned m = __match_any_sync(0xffffffffu, ls);
@@ -275,7 +274,10 @@ __global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_co
     const uint32_t per = (nst + blockDim.x - 1) / blockDim.x;
     const uint32_t i0 = min(nst, threadIdx.x * per), i1 = min(nst, i0 + per);
     uint32_t nlive = 0;
-    for (uint32_t i = i0; i < i1; i++) nlive += T.gslot[stage[i] >> 13] != INVALID;
+    for (uint32_t i = i0; i < i1; i++) {
+        const uint32_t e = stage[i];
+        nlive += !(e & STAGE_DIRECT) && T.gslot[(e >> 13) & 255] != INVALID;
+    }
     uint32_t total;
     const uint32_t off = block_exclusive_scan_u32(nlive, red, &total);
     if (threadIdx.x == 0) {
@@ -285,13 +287,14 @@ __global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_co
         s_base = b;
     }
     __syncthreads();
-    uint32_t pos = s_base + off;
+    uint32_t at = s_base + off;
     for (uint32_t i = i0; i < i1; i++) {
         const uint32_t e = stage[i];
-        const uint32_t gs = T.gslot[e >> 13];
+        if (e & STAGE_DIRECT) continue;
+        const uint32_t gs = T.gslot[(e >> 13) & 255];
         if (gs == INVALID) continue;
-        if (pos < F.point_cap) F.points[pos] = ((unsigned long long)gs << 32) | stage_packed(e, x0, y0);
-        pos++;
+        if (at < F.point_cap) F.points[at] = ((unsigned long long)gs << 32) | stage_packed(e, x0, y0);
+        at++;
     }
 }
 
@@ -680,7 +683,7 @@ __global__ void __launch_bounds__(1024) k_peaks_scan(const __grid_constant__ Fra
 __global__ void __launch_bounds__(256) k_index_quads(const __grid_constant__ FrameSet fs,
                                                      const uint32_t* __restrict__ work_offsets, uint32_t n_frames,
                                                      PipelineParams p) {
-    __shared__ unsigned long long red64[32];
+    __shared__ SegmentTable T;
     __shared__ uint32_t red32[33];
     const uint32_t total = work_offsets[n_frames];
     for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
@@ -688,22 +691,17 @@ __global__ void __launch_bounds__(256) k_index_quads(const __grid_constant__ Fra
         const FrameDesc& F = fs.get(fidx);
         const uint32_t q = item - work_offsets[fidx];
         const uint32_t cid = F.peak_clusters[q];
-        const atag_peak_extents pe{0u, F.peak_count[cid]};
         const atag_cluster_extents ce = F.cluster_extents[p.compat_peak_index ? q : cid];
-        Combination c = evaluate_combination(threadIdx.x, pe, F.peaks + (size_t)cid * 10, F.line_fit + ce.start,
-                                             ce.count, p.max_line_fit_mse, p.cos_critical_f);
-        int chosen = choose_combination(c.err, threadIdx.x, red64, red32);
+        atag_fitted_quad* fq = F.fitted + q;
+        const int chosen = index_one_cluster(F.peak_count[cid], F.peaks + (size_t)cid * 10, F.line_fit + ce.start,
+                                             ce.count, p.max_line_fit_mse, p.cos_critical_f, T, red32, fq);
         if (chosen < 0) {
-            if (threadIdx.x == 0) {
-                Combination z;
-                for (int s = 0; s < 4; s++) { z.m[s] = Moment{0, 0, 0, 0, 0, 0}; z.nim[s] = 0; z.idx[s] = 0; }
-                write_fitted(F.fitted + q, z);
-                F.quad_ok[q] = 0;
-            }
+            // no combination: the quad stays zero (main.cpp:318-319)
+            if (threadIdx.x < sizeof(atag_fitted_quad) / 4) reinterpret_cast<uint32_t*>(fq)[threadIdx.x] = 0u;
+            if (threadIdx.x == 0) F.quad_ok[q] = 0;
         } else if ((int)threadIdx.x == chosen) {
-            write_fitted(F.fitted + q, c);
             atag_quad_corners qc;
-            bool ok = quad_corners(F.fitted[q], p, q, &qc);
+            bool ok = quad_corners(*fq, p, q, &qc);
             F.quad_tmp[q] = qc;
             F.quad_ok[q] = ok ? 1u : 0u;
         }

@@ -309,15 +309,15 @@ __global__ void __launch_bounds__(256) k_ccl_final(const __grid_constant__ Frame
     const int nbx = w / 2, nb = nbx * (h / 2);
     volatile uint32_t* par = F.scratch;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
-        int bx = i % nbx, by = i / nbx;
-        size_t id = (size_t)(by * 2) * w + bx * 2;
-        uint32_t sw = (uint32_t)id, sb = (uint32_t)id + 1;
-        uint32_t rw = find_root_volatile(par, sw), rb = find_root_volatile(par, sb);
+        const int bx = i % nbx, by = i / nbx;
+        const size_t id = (size_t)(by * 2) * w + bx * 2;
+        const uint32_t sw = (uint32_t)id, sb = (uint32_t)id + 1;
+        const uint32_t rw = find_root_volatile(par, sw), rb = find_root_volatile(par, sb);
         // compress: every slot ends pointing at its root, as the reference's
         // scratch does after its last compression (segmentation.cpp:309)
         par[sw] = rw;
         par[sb] = rb;
-        uint32_t cw = F.sizes[sw], cb = F.sizes[sb];
+        const uint32_t cw = F.sizes[sw], cb = F.sizes[sb];
         if (rw != sw) {
             if (cw) atomicAdd(F.sizes + rw, cw);
             F.sizes[sw] = 0;
@@ -327,9 +327,9 @@ __global__ void __launch_bounds__(256) k_ccl_final(const __grid_constant__ Frame
             F.sizes[sb] = 0;
         }
         const uint8_t* t = F.thr + id;
-        uchar2 top = *reinterpret_cast<const uchar2*>(t);
-        uchar2 bot = *reinterpret_cast<const uchar2*>(t + w);
-        auto lab = [&](uint8_t v) { return v == 255 ? (LABEL_PIXEL_MASK | rw) : (v == 0 ? rb : 0u); };
+        const uchar2 top = *reinterpret_cast<const uchar2*>(t);
+        const uchar2 bot = *reinterpret_cast<const uchar2*>(t + w);
+        auto lab = [&](uint8_t c) { return c == 255 ? (LABEL_PIXEL_MASK | rw) : (c == 0 ? rb : 0u); };
         *reinterpret_cast<uint2*>(F.labels + id) = make_uint2(lab(top.x), lab(top.y));
         *reinterpret_cast<uint2*>(F.labels + id + w) = make_uint2(lab(bot.x), lab(bot.y));
     }

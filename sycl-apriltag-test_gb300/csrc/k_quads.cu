@@ -83,15 +83,13 @@ __global__ void __launch_bounds__(256) k_do_indexing(const atag_peak_extents* __
                                                      const atag_cluster_extents* __restrict__ cluster_extents,
                                                      float max_mse, float cos_critical,
                                                      atag_fitted_quad* __restrict__ fitted) {
-    __shared__ unsigned long long red[32];
+    __shared__ SegmentTable T;
     __shared__ uint32_t redu[33];
     for (size_t q = blockIdx.x; q < count; q += gridDim.x) {
         const atag_peak_extents pe = extents[q];
         const atag_cluster_extents ce = cluster_extents[q];
-        Combination c = evaluate_combination(threadIdx.x, pe, corners, points + ce.start, ce.count,
-                                             max_mse, cos_critical);
-        int chosen = choose_combination(c.err, threadIdx.x, red, redu);
-        if (chosen >= 0 && (int)threadIdx.x == chosen) write_fitted(fitted + q, c);
+        index_one_cluster(pe.count, corners + pe.start, points + ce.start, ce.count, max_mse, cos_critical, T, redu,
+                          fitted + q);
         __syncthreads();
     }
 }
