@@ -80,3 +80,30 @@ def test_calls_without_device_return_status(monkeypatch):
     assert L.atag_last_error()
     st = L.atag_threshold_image(None, None, None, None, 64, 64, None)
     assert st == 5
+
+
+def test_cpp_header_compiles_against_the_c_abi(tmp_path):
+    """include/atag.hpp (reference-named C++ wrappers) compiles and links
+    against the library (no device needed to link)."""
+    import os
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "use.cpp"
+    src.write_text('#include "atag.hpp"\n'
+                   "int main() {\n"
+                   "  cudaStream_t q = nullptr;\n"
+                   "  atag_status s = atag::threshold_image(q, nullptr, nullptr, nullptr, nullptr, 6, 6);\n"
+                   "  return s == ATAG_ERR_INVALID_ARGUMENT || s == ATAG_ERR_NO_DEVICE ? 0 : 1;\n"
+                   "}\n")
+    lib.load()
+    libdir = os.path.dirname(lib.LIB_PATH)
+    cuda_inc = "/usr/local/cuda/include"
+    r = subprocess.run(["g++", "-std=c++17", "-I", os.path.join(root, "include"), "-I", cuda_inc, str(src),
+                        "-L", libdir, "-latag_gb300", f"-Wl,-rpath,{libdir}", "-o", str(tmp_path / "use")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(tmp_path / "use")], capture_output=True, text=True)
+    assert r.returncode == 0
