@@ -40,8 +40,28 @@ def _render(seed):
     return synth.render(synth.CONFIGS["1080p"], seed)
 
 
+def _render_spec(args):
+    spec, seed = args
+    sys.path.insert(0, PKG)
+    from atag import synth
+    return synth.render(spec, seed)
+
+
 def render_frames(n, seed0, pool):
     return list(pool.map(_render, [seed0 + i for i in range(n)]))
+
+
+def mixed_specs(n, seed):
+    sys.path.insert(0, PKG)
+    from atag import synth
+    return synth.batch_specs(n, seed)
+
+
+def camera_specs():
+    sys.path.insert(0, PKG)
+    from atag import synth
+    return [synth.FrameSpec(1280, 720, 20, (16, 200), 150, (0.5, 1.5), (2.0, 8.0))] * 4 + \
+        [synth.FrameSpec(1920, 1080, 40, (16, 300), 300, (0.5, 1.5), (2.0, 8.0))] * 4
 
 
 class ClockSampler:
@@ -179,6 +199,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--ref-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mixed", type=int, default=64, help="frames of the mixed-resolution batch (0 = skip)")
+    ap.add_argument("--refine-quads", type=int, default=4096, help="quads of the refinement step (0 = skip)")
+    ap.add_argument("--serving-seconds", type=float, default=5.0, help="length of the serving run (0 = skip)")
+    ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -190,9 +214,17 @@ def main():
 
     # render frames before touching the GPU (spawned workers)
     n_render = max(args.batch, args.cpu_sample if rank == 0 and world == 1 and not args.no_cpu else 0)
+    extra_n = args.mixed if world == 1 else 0
     with concurrent.futures.ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1),
                                                 mp_context=mp.get_context("spawn")) as pool:
         host_frames = render_frames(n_render, 1000 + rank * 100000, pool)
+        specs = mixed_specs(extra_n, 77) if extra_n else []
+        mixed_frames = list(pool.map(_render_spec, [(sp, 5000 + i) for i, sp in enumerate(specs)]))
+        cam_frames = []
+        if args.serving_seconds > 0 and world == 1:
+            cs = camera_specs()
+            flat = list(pool.map(_render_spec, [(sp, 9000 + 10 * c + k) for c, sp in enumerate(cs) for k in range(2)]))
+            cam_frames = [flat[2 * c: 2 * c + 2] for c in range(len(cs))]
 
     import numpy as np
     import torch
@@ -215,6 +247,10 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
+    tuning = None
+    if not args.no_tune:
+        from atag import autotune
+        tuning = autotune.autotune(det, frames, reps=3, passes=1)
     # --- validate + warm (eager)
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -336,6 +372,82 @@ def main():
     e2e = {"value": B * args.steps * world / dt, "unit": "frames/s", "h2d_bytes_per_step": B * W * H,
            "d2h_bytes_per_step": h_stats.numel() + h_quads.numel()}
 
+    # --- mixed-resolution batch (64 frames, 640x480 .. 2592x1944), one graph
+    mixed = None
+    if mixed_frames:
+        mw, mh = max(f.shape[1] for f in mixed_frames), max(f.shape[0] for f in mixed_frames)
+        mtot = sum(f.size for f in mixed_frames)
+        detm = Detector(mw // args.decimate, mh // args.decimate, max_frames=len(mixed_frames),
+                        max_total_pixels=mtot // (args.decimate ** 2) + 4096, config=cfg)
+        mframes = [torch.from_numpy(f).cuda() for f in mixed_frames]
+        mtune = None
+        if not args.no_tune:
+            from atag import autotune
+            mtune = autotune.autotune(detm, mframes, reps=2, passes=1)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                detm.enqueue(mframes, stream=stream)
+        stream.synchronize()
+        gm = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gm, stream=stream):
+            detm.enqueue(mframes, stream=stream)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                gm.replay()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(args.steps):
+                gm.replay()
+            b.record(stream)
+        b.synchronize()
+        mms = a.elapsed_time(b) / args.steps
+        mst = detm.stats()
+        mixed = {"frames_per_step": len(mframes), "ms_per_step": mms, "frames_per_s": 1000.0 * len(mframes) / mms,
+                 "megapixels_per_s": mtot / 1e6 / (mms / 1000.0),
+                 "status_ok": all(int(x["status"]) == 0 for x in mst),
+                 "quads_per_frame": statistics.mean(int(x["n_quads"]) for x in mst),
+                 "tuning": mtune["tuning"] if mtune else None}
+        del detm, gm
+
+    # --- corner refinement: forward + hand-written adjoint on 4096 quads
+    refine_line = None
+    if args.refine_quads > 0:
+        from atag import refine
+        g = torch.Generator(device="cpu").manual_seed(3)
+        img = torch.from_numpy(host_frames[0]).float().div(255.0).cuda()
+        nq = args.refine_quads
+        ctr = torch.rand((nq, 1, 2), generator=g) * torch.tensor([W - 200.0, H - 200.0]) + 100.0
+        sq = torch.tensor([[-1.0, -1.0], [1.0, -1.0], [1.0, 1.0], [-1.0, 1.0]])
+        quads_c = (ctr + sq[None] * (torch.rand((nq, 1, 1), generator=g) * 40 + 10)).cuda()
+        gref = torch.randn((nq, 4, 2), generator=g).cuda()
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                refine.refine_forward(img, quads_c)
+                refine.refine_backward(img, quads_c, gref, None)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(args.steps):
+                refine.refine_forward(img, quads_c)
+                refine.refine_backward(img, quads_c, gref, None)
+            b.record(stream)
+        b.synchronize()
+        rms = a.elapsed_time(b) / args.steps
+        refine_line = {"quads": nq, "samples_per_quad": 256, "ms_fwd_bwd": rms,
+                       "quads_per_s": nq / (rms / 1000.0)}
+
+    # --- serving: 8 cameras (4 x 720p60, 4 x 1080p30), Poisson arrivals
+    serving_line = None
+    if cam_frames:
+        from atag import serving
+        slots = [serving.DetectorExecutor(W, H, max_frames=8, max_total_pixels=8 * W * H) for _ in range(3)]
+        srv = serving.Server(slots)
+        rates = [60.0] * 4 + [30.0] * 4
+        res = serving.run_cameras(srv, cam_frames, rates, duration_s=args.serving_seconds, seed=1)
+        serving_line = serving.latency_summary(res, args.serving_seconds)
+        serving_line["cameras"] = "4x1280x720@60 + 4x1920x1080@30"
+        serving_line["slots"] = len(slots)
+        del slots, srv
+
     # --- CPU baseline (rank 0, N=1)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -362,6 +474,10 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "plain": plain,
         "batched_vs_plain": value / world / plain["frames_per_s"],
+        "mixed_batch": mixed,
+        "refine": refine_line,
+        "serving": serving_line,
+        "tuning": tuning["tuning"] if tuning else None,
         "roofline": roofline,
         "stages_ms_per_step": stage_ms,
         "cpu_baseline": cpu,

@@ -324,6 +324,49 @@ atag_status atag_use_device(int ordinal);
 
 atag_status atag_detector_views(const atag_detector *det, size_t frame, atag_frame_views *out);
 
+/* ------------------------------------------------------------------ */
+/* Subpixel corner refinement (no counterpart in the reference, which  */
+/* stops at the corners of process_fitted_quads, src/main.cpp:1035).    */
+/* ------------------------------------------------------------------ */
+/* Per quad and edge (corner i -> corner i+1): 16 positions along the edge,
+ * 4 bilinear taps of the FP32 image across it at -1.5, -0.5, 0.5, 1.5 px
+ * (64 samples), an edge point per position offset along the normal by the
+ * strength-weighted mean of the tap differences, a weighted line fit of the
+ * 16 points (weight: edge strength + 1e-6, so a flat edge keeps its line) (FP32 moments about the edge midpoint, FP64 2x2 eigen-solve),
+ * and refined corner i = intersection of edge lines i-1 and i (FP64).
+ * corners/refined: n_quads x 4 x 2 floats (x, y); residual: n_quads x 4
+ * (weight sum times the smallest covariance eigenvalue: the weighted
+ * line-fit residual); samples: n_quads x 4 x 64 (may be NULL). */
+atag_status atag_refine_forward(const float *d_image, size_t width, size_t height, const float *d_corners,
+                                size_t n_quads, float *d_refined, float *d_residual, float *d_samples,
+                                atag_stream_t stream);
+/* Adjoint of atag_refine_forward: given dL/d(refined) and dL/d(residual)
+ * (either may be NULL = zero), writes dL/d(corners) (n_quads x 8),
+ * dL/d(samples) (n_quads x 4 x 64, may be NULL) and accumulates dL/d(image)
+ * into d_grad_image (width x height, may be NULL; caller zeroes it). */
+atag_status atag_refine_backward(const float *d_image, size_t width, size_t height, const float *d_corners,
+                                 size_t n_quads, const float *d_grad_refined, const float *d_grad_residual,
+                                 float *d_grad_corners, float *d_grad_samples, float *d_grad_image,
+                                 atag_stream_t stream);
+
+/* Launch shapes of the detector's kernels.  Every choice gives the same
+ * results; only the speed changes.  atag_detector_create starts from the
+ * defaults below; the autotuner (sycl-apriltag-test_gb300/atag/autotune.py)
+ * picks them per GPU and workload. */
+typedef struct atag_tuning {
+    int32_t ccl_tile_rows;        /* 8 or 16 rows of 2x2 blocks per CCL tile (16)   */
+    int32_t boundary_tile_rows;   /* 8 or 16 pixel rows per boundary tile (16)      */
+    int32_t small_cluster_max;    /* clusters up to this size use the 128-thread
+                                     kernel, larger ones the 512-thread one
+                                     (1..4096, default 4096)                        */
+    int32_t small_ctas_per_sm;    /* persistent CTAs of the small-cluster kernel (4) */
+    int32_t large_ctas_divisor;   /* large-cluster CTAs = SMs / divisor (4)         */
+    int32_t index_ctas_per_sm;    /* CTAs of the combination search per SM (8)      */
+} atag_tuning;
+
+atag_status atag_detector_get_tuning(const atag_detector *det, atag_tuning *out);
+atag_status atag_detector_set_tuning(atag_detector *det, const atag_tuning *tuning);
+
 /* Stage timing.  When set, every later detect call records events[i] (a
  * cudaEvent_t) on its stream just before stage i and events[ATAG_STAGE_COUNT]
  * after the last, so cudaEventElapsedTime(events[i], events[i+1]) is stage

@@ -79,6 +79,31 @@ inline atag_status process_fitted_quads(cudaStream_t q, const FittedQuad* fitted
     return atag_process_fitted_quads(fitted, count, width, height, cfg, out, capacity, d_count, as_stream(q));
 }
 
+// Corner refinement as a forward/backward pair with the contract of
+// torch.autograd.Function: forward saves what backward needs in a context,
+// backward maps output gradients to input gradients.
+struct RefineContext {
+    const float* image = nullptr;
+    size_t width = 0, height = 0;
+    const float* corners = nullptr;
+    size_t n_quads = 0;
+};
+
+struct CornerRefine {
+    static atag_status forward(RefineContext& ctx, cudaStream_t q, const float* image, size_t width, size_t height,
+                               const float* corners, size_t n_quads, float* refined, float* residual,
+                               float* samples = nullptr) {
+        ctx = RefineContext{image, width, height, corners, n_quads};
+        return atag_refine_forward(image, width, height, corners, n_quads, refined, residual, samples, as_stream(q));
+    }
+    static atag_status backward(const RefineContext& ctx, cudaStream_t q, const float* grad_refined,
+                                const float* grad_residual, float* grad_corners, float* grad_samples = nullptr,
+                                float* grad_image = nullptr) {
+        return atag_refine_backward(ctx.image, ctx.width, ctx.height, ctx.corners, ctx.n_quads, grad_refined,
+                                    grad_residual, grad_corners, grad_samples, grad_image, as_stream(q));
+    }
+};
+
 // RAII owner of an atag_detector (the whole path of src/main.cpp:322-1024).
 class Detector {
 public:

@@ -94,6 +94,21 @@ class Detector:
                   "atag_detect_host")
         return out[: int(st[0]["n_quads"])], st[0]
 
+    # -- launch shapes -------------------------------------------------------
+    def get_tuning(self) -> dict:
+        from .records import Tuning
+        t = Tuning()
+        lib.check(self.L.atag_detector_get_tuning(self.handle, ctypes.byref(t)), "get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, **fields):
+        from .records import Tuning
+        t = Tuning()
+        lib.check(self.L.atag_detector_get_tuning(self.handle, ctypes.byref(t)), "get_tuning")
+        for k, v in fields.items():
+            setattr(t, k, int(v))
+        lib.check(self.L.atag_detector_set_tuning(self.handle, ctypes.byref(t)), "set_tuning")
+
     # -- stage timing --------------------------------------------------------
     def set_stage_events(self, events):
         """events: lib.STAGE_COUNT + 1 torch.cuda.Event(enable_timing=True)

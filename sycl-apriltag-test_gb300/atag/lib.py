@@ -7,7 +7,7 @@ import ctypes
 import os
 import re
 
-from .records import Config, Frame, FrameViews
+from .records import Config, Frame, FrameViews, Tuning
 
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_ROOT, "lib", "libatag_gb300.so")
@@ -47,6 +47,10 @@ _SIGNATURES = {
     "atag_detector_views": (_ST, [_P, _SZ, ctypes.POINTER(FrameViews)]),
     "atag_detector_set_stage_events": (_ST, [_P, ctypes.POINTER(_P), _SZ]),
     "atag_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "atag_detector_get_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
+    "atag_detector_set_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
+    "atag_refine_forward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P]),
+    "atag_refine_backward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P, _P, _P]),
 }
 STAGE_COUNT = 13
 

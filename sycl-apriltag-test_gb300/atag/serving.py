@@ -1,0 +1,213 @@
+"""Continuous-batching request loop for multi-camera quad detection.
+
+Requests (one frame each, host memory) arrive at any time.  The server owns
+a pool of *slots*; each slot is one in-flight micro-batch with its own CUDA
+stream and a detector whose workspace (thresholded image, union-find forest,
+labels, sizes, pair tables, cluster buffers) stays resident for the life of
+the server.  The number of slots is chosen from the free device memory at
+start-up (admission by memory), and each slot admits frames up to its pixel
+budget.  Whenever a slot is free, every request that has arrived since is
+admitted into it; slots run concurrently on the device, so requests that
+arrive while others are on the GPU overlap with them.  Latency is measured
+from arrival to the moment the slot's results are back on the host.
+
+The scheduler is independent of CUDA: it drives objects with the Executor
+interface (`launch`, `done`, `results`), so its logic is tested on the CPU
+with a fake executor and run on the GPU with DetectorExecutor.
+"""
+import collections
+import heapq
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Request:
+    seq: int
+    camera: int
+    frame: np.ndarray          # H x W uint8, source resolution
+    t_arrival: float           # seconds, on the server clock
+
+
+@dataclass
+class Result:
+    seq: int
+    camera: int
+    quads: np.ndarray          # QUAD_CORNERS records
+    stats: np.void
+    t_arrival: float
+    t_done: float
+    batch_size: int
+
+    @property
+    def latency_ms(self):
+        return 1000.0 * (self.t_done - self.t_arrival)
+
+
+class DetectorExecutor:
+    """One slot on the GPU: resident detector + stream + pinned staging."""
+
+    def __init__(self, max_width, max_height, max_frames, max_total_pixels, config=None, quad_capacity=256,
+                 src_factor=1):
+        import torch
+
+        from .detector import Detector
+        self.torch = torch
+        self.det = Detector(max_width, max_height, max_frames=max_frames, max_total_pixels=max_total_pixels,
+                            config=config, quad_capacity=quad_capacity)
+        self.stream = torch.cuda.Stream()
+        src_px = max_total_pixels * src_factor * src_factor
+        self.h_in = torch.empty(src_px, dtype=torch.uint8).pin_memory()
+        self.d_in = torch.empty(src_px, dtype=torch.uint8, device="cuda")
+        self.h_stats = torch.empty(self.det.d_stats.numel(), dtype=torch.uint8).pin_memory()
+        self.h_quads = torch.empty(self.det.d_quads.numel(), dtype=torch.uint8).pin_memory()
+        self.event = torch.cuda.Event()
+        self.max_frames = max_frames
+        self.max_pixels = src_px
+        self.n = 0
+
+    def capacity(self):
+        return self.max_frames, self.max_pixels
+
+    def launch(self, frames):
+        torch = self.torch
+        off = 0
+        views = []
+        for f in frames:
+            n = f.size
+            self.h_in[off:off + n].numpy()[:] = f.reshape(-1)
+            views.append((off, f.shape))
+            off += n
+        with torch.cuda.stream(self.stream):
+            self.d_in[:off].copy_(self.h_in[:off], non_blocking=True)
+            dev = [self.d_in[o:o + s[0] * s[1]].view(s[0], s[1]) for o, s in views]
+            self.det.enqueue(dev, stream=self.stream)
+            self.h_stats.copy_(self.det.d_stats, non_blocking=True)
+            self.h_quads.copy_(self.det.d_quads, non_blocking=True)
+            self.event.record(self.stream)
+        self.n = len(frames)
+
+    def done(self):
+        return self.event.query()
+
+    def results(self):
+        from .records import FRAME_STATS, QUAD_CORNERS
+        self.event.synchronize()
+        st = self.h_stats.numpy()[: self.n * FRAME_STATS.itemsize].view(FRAME_STATS)
+        q = self.h_quads.numpy().view(QUAD_CORNERS).reshape(self.det.max_frames, self.det.quad_capacity)
+        return [(q[i, : int(st[i]["n_quads"])].copy(), st[i].copy()) for i in range(self.n)]
+
+
+def slots_for_memory(free_bytes, slot_bytes, fraction=0.5, max_slots=8):
+    """Admission by device memory: how many resident slots fit in
+    `fraction` of the free memory (at least one)."""
+    return int(max(1, min(max_slots, (free_bytes * fraction) // max(slot_bytes, 1))))
+
+
+class Server:
+    """Continuous batching over a pool of executors (slots)."""
+
+    def __init__(self, executors, clock=time.perf_counter):
+        self.slots = list(executors)
+        self.busy = [None] * len(self.slots)   # list of requests in flight per slot
+        self.queue = collections.deque()
+        self.clock = clock
+        self.t0 = clock()
+        self.completed = []
+        self.max_in_flight = 0
+
+    def now(self):
+        return self.clock() - self.t0
+
+    def submit(self, req: Request):
+        self.queue.append(req)
+
+    def _admit(self):
+        for i, ex in enumerate(self.slots):
+            if self.busy[i] is not None or not self.queue:
+                continue
+            max_frames, max_pixels = ex.capacity()
+            take, px = [], 0
+            while self.queue and len(take) < max_frames and px + self.queue[0].frame.size <= max_pixels:
+                r = self.queue.popleft()
+                take.append(r)
+                px += r.frame.size
+            if not take:  # a single frame larger than the slot's budget
+                raise ValueError("frame exceeds the slot pixel budget")
+            ex.launch([r.frame for r in take])
+            self.busy[i] = take
+        self.max_in_flight = max(self.max_in_flight, sum(b is not None for b in self.busy))
+
+    def _reap(self):
+        for i, ex in enumerate(self.slots):
+            reqs = self.busy[i]
+            if reqs is None or not ex.done():
+                continue
+            out = ex.results()
+            t = self.now()
+            for r, (quads, stats) in zip(reqs, out):
+                self.completed.append(Result(r.seq, r.camera, quads, stats, r.t_arrival, t, len(reqs)))
+            self.busy[i] = None
+
+    def poll(self):
+        self._reap()
+        self._admit()
+
+    def idle(self):
+        return not self.queue and all(b is None for b in self.busy)
+
+    def drain(self, timeout_s=60.0):
+        end = self.now() + timeout_s
+        while not self.idle():
+            self.poll()
+            if self.now() > end:
+                raise TimeoutError("server did not drain")
+
+
+@dataclass(order=True)
+class _Arrival:
+    t: float
+    seq: int
+    camera: int = field(compare=False)
+
+
+def poisson_arrivals(rates_hz, duration_s, seed):
+    """Merged Poisson arrival times of several cameras: [(t, camera)]."""
+    rng = np.random.default_rng(seed)
+    heap = []
+    for cam, rate in enumerate(rates_hz):
+        t = rng.exponential(1.0 / rate)
+        while t < duration_s:
+            heap.append((t, cam))
+            t += rng.exponential(1.0 / rate)
+    heap.sort()
+    return heap
+
+
+def run_cameras(server: Server, camera_frames, rates_hz, duration_s, seed=0, on_result=None):
+    """Replays Poisson arrivals in real time: camera c submits
+    camera_frames[c][k % len] at each of its arrival times.  Returns the
+    completed results sorted by sequence number."""
+    arrivals = poisson_arrivals(rates_hz, duration_s, seed)
+    counters = collections.Counter()
+    seq = 0
+    server.t0 = server.clock()
+    for t, cam in arrivals:
+        while server.now() < t:
+            server.poll()
+        frames = camera_frames[cam]
+        server.submit(Request(seq, cam, frames[counters[cam] % len(frames)], server.now()))
+        counters[cam] += 1
+        seq += 1
+        server.poll()
+    server.drain()
+    return sorted(server.completed, key=lambda r: r.seq)
+
+
+def latency_summary(results, duration_s):
+    lat = np.array([r.latency_ms for r in results]) if results else np.zeros(1)
+    return {"requests": len(results), "frames_per_s": len(results) / duration_s,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "max_ms": float(lat.max()), "mean_batch": float(np.mean([r.batch_size for r in results]) if results else 0)}

@@ -112,8 +112,11 @@ struct PipelineParams {
 // k_pixels.cu
 __global__ void k_decimate(const __grid_constant__ FrameSet fs);
 __global__ void k_threshold(const __grid_constant__ FrameSet fs, int min_diff, int write_extrema);
-__global__ void k_ccl_local(const __grid_constant__ FrameSet fs);
-__global__ void k_ccl_border(const __grid_constant__ FrameSet fs);
+// CCL tiles of 32 x 8 or 32 x 16 blocks (2x2 pixels)
+__global__ void k_ccl_local_r8(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_local_r16(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_border_r8(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_border_r16(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_final(const __grid_constant__ FrameSet fs);
 __global__ void k_boundaries_dense(const __grid_constant__ FrameSet fs, uint32_t min_size);
 
@@ -128,8 +131,10 @@ __global__ void k_process_quads(const atag_fitted_quad* fitted, size_t count, Pi
 
 // k_cluster.cu (fused path)
 __global__ void k_reset_frames(const __grid_constant__ FrameSet fs);
-__global__ void k_boundaries_pairs(const __grid_constant__ FrameSet fs, uint32_t min_size);
-__global__ void k_pairs_finalize(const __grid_constant__ FrameSet fs, PipelineParams p);
+// boundary tiles of 64 x 8 or 64 x 16 pixels
+__global__ void k_boundaries_pairs_r8(const __grid_constant__ FrameSet fs, uint32_t min_size);
+__global__ void k_boundaries_pairs_r16(const __grid_constant__ FrameSet fs, uint32_t min_size);
+__global__ void k_pairs_finalize(const __grid_constant__ FrameSet fs, PipelineParams p, uint32_t small_max);
 __global__ void k_scatter_points(const __grid_constant__ FrameSet fs);
 __global__ void k_cluster_fit_small(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets,
                                     uint32_t n_frames, uint32_t* work_counter);

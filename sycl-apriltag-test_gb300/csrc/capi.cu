@@ -233,6 +233,7 @@ struct atag_detector {
     std::vector<FrameDesc> last;     // table last uploaded
     std::vector<FrameDesc> cur;      // table of the last call
     std::vector<cudaEvent_t> stage_events;
+    atag_tuning tuning{16, 16, (int32_t)CF_SMALL_CAP, 4, 4, 8};
 };
 
 namespace {
@@ -335,13 +336,21 @@ atag_status atag_threshold_image(const uint8_t* grey, uint8_t* extrema, uint8_t*
     return ATAG_OK;
 }
 
-static atag_status launch_segmentation(const FrameSet& fs, size_t max_w, size_t max_h, size_t nf, cudaStream_t s) {
-    size_t tiles = cdiv(max_w / 2, 32) * cdiv(max_h / 2, 16);
-    k_ccl_local<<<grid2(tiles, nf), 512, 0, s>>>(fs);
-    LAUNCHED();
-    size_t border = tiles * (32 + 2 * (16 - 1));
-    k_ccl_border<<<grid2(cdiv(border, 256), nf), 256, 0, s>>>(fs);
-    LAUNCHED();
+static atag_status launch_segmentation(const FrameSet& fs, size_t max_w, size_t max_h, size_t nf, cudaStream_t s,
+                                       int rows = 16) {
+    size_t tiles = cdiv(max_w / 2, 32) * cdiv(max_h / 2, (size_t)rows);
+    size_t border = tiles * (32 + 2 * (rows - 1));
+    if (rows == 8) {
+        k_ccl_local_r8<<<grid2(tiles, nf), 32 * 8, 0, s>>>(fs);
+        LAUNCHED();
+        k_ccl_border_r8<<<grid2(cdiv(border, 256), nf), 256, 0, s>>>(fs);
+        LAUNCHED();
+    } else {
+        k_ccl_local_r16<<<grid2(tiles, nf), 32 * 16, 0, s>>>(fs);
+        LAUNCHED();
+        k_ccl_border_r16<<<grid2(cdiv(border, 256), nf), 256, 0, s>>>(fs);
+        LAUNCHED();
+    }
     size_t blocks = (max_w / 2) * (max_h / 2);
     k_ccl_final<<<grid2(std::min<size_t>(cdiv(blocks, 256), 8192), nf), 256, 0, s>>>(fs);
     LAUNCHED();
@@ -583,7 +592,10 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
         return ATAG_OK;
     };
 #define STAGE(i) do { atag_status m_ = mark(i); if (m_) return m_; } while (0)
-    const size_t tiles_ccl = cdiv(mw / 2, 32) * cdiv(mh / 2, 16);
+    const atag_tuning& tu = det->tuning;
+    const int ccl_rows = tu.ccl_tile_rows == 8 ? 8 : 16;
+    const int bp_rows = tu.boundary_tile_rows == 8 ? 8 : 16;
+    const size_t tiles_ccl = cdiv(mw / 2, 32) * cdiv(mh / 2, (size_t)ccl_rows);
     STAGE(0);
     k_reset_frames<<<grid2(cdiv(max_pair, 256), n), 256, 0, s>>>(fs);
     LAUNCHED();
@@ -596,19 +608,27 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     k_threshold<<<grid2(cdiv(mw / 4, 32) * cdiv(mh / 4, 8), n), 256, 0, s>>>(fs, p.min_white_black_diff, 0);
     LAUNCHED();
     STAGE(3);
-    k_ccl_local<<<grid2(tiles_ccl, n), 512, 0, s>>>(fs);
+    if (ccl_rows == 8) k_ccl_local_r8<<<grid2(tiles_ccl, n), 32 * 8, 0, s>>>(fs);
+    else k_ccl_local_r16<<<grid2(tiles_ccl, n), 32 * 16, 0, s>>>(fs);
     LAUNCHED();
     STAGE(4);
-    k_ccl_border<<<grid2(cdiv(tiles_ccl * (32 + 2 * (16 - 1)), 256), n), 256, 0, s>>>(fs);
-    LAUNCHED();
+    {
+        const size_t border = tiles_ccl * (32 + 2 * (ccl_rows - 1));
+        if (ccl_rows == 8) k_ccl_border_r8<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
+        else k_ccl_border_r16<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
+        LAUNCHED();
+    }
     STAGE(5);
     k_ccl_final<<<grid2(std::min<size_t>(cdiv((mw / 2) * (mh / 2), 256), 8192), n), 256, 0, s>>>(fs);
     LAUNCHED();
     STAGE(6);
-    k_boundaries_pairs<<<grid2(cdiv(mw, 64) * cdiv(mh, 16), n), 256, 0, s>>>(fs, p.min_component_size);
+    if (bp_rows == 8)
+        k_boundaries_pairs_r8<<<grid2(cdiv(mw, 64) * cdiv(mh, 8), n), 16 * 8, 0, s>>>(fs, p.min_component_size);
+    else
+        k_boundaries_pairs_r16<<<grid2(cdiv(mw, 64) * cdiv(mh, 16), n), 16 * 16, 0, s>>>(fs, p.min_component_size);
     LAUNCHED();
     STAGE(7);
-    k_pairs_finalize<<<(unsigned)n, 1024, 0, s>>>(fs, p);
+    k_pairs_finalize<<<(unsigned)n, 1024, 0, s>>>(fs, p, (uint32_t)tu.small_cluster_max);
     LAUNCHED();
     k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_SMALL, off_small, CNT_LARGE, off_large, wc);
     LAUNCHED();
@@ -619,10 +639,11 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     // large clusters on the side stream, concurrently with the small ones
     CK(cudaEventRecord(det->fork, s));
     CK(cudaStreamWaitEvent(det->side, det->fork, 0));
-    k_cluster_fit_large<<<std::max(1, sms / 4), CF_LARGE_THREADS, CF_LARGE_SMEM, det->side>>>(fs, off_large,
+    k_cluster_fit_large<<<std::max(1, sms / std::max(1, tu.large_ctas_divisor)), CF_LARGE_THREADS, CF_LARGE_SMEM,
+                          det->side>>>(fs, off_large,
                                                                                                 (uint32_t)n, wc + 1);
     LAUNCHED();
-    k_cluster_fit_small<<<sms * 4, CF_SMALL_THREADS, CF_SMALL_SMEM, s>>>(
+    k_cluster_fit_small<<<sms * std::max(1, tu.small_ctas_per_sm), CF_SMALL_THREADS, CF_SMALL_SMEM, s>>>(
         fs, off_small, (uint32_t)n, wc);
     LAUNCHED();
     CK(cudaEventRecord(det->join, det->side));
@@ -633,7 +654,7 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_PEAKCLU, off_peaks, 0, nullptr, wc + 2);
     LAUNCHED();
     STAGE(11);
-    k_index_quads<<<sms * 8, 256, 0, s>>>(fs, off_peaks, (uint32_t)n, p);
+    k_index_quads<<<sms * std::max(1, tu.index_ctas_per_sm), 256, 0, s>>>(fs, off_peaks, (uint32_t)n, p);
     LAUNCHED();
     STAGE(12);
     k_compact_quads<<<(unsigned)n, 1024, 0, s>>>(fs);
@@ -703,6 +724,25 @@ atag_status atag_detector_set_stage_events(atag_detector* det, void* const* even
     if (n != ATAG_STAGE_COUNT + 1)
         return fail(ATAG_ERR_INVALID_ARGUMENT, "set_stage_events: need %d events, got %zu", ATAG_STAGE_COUNT + 1, n);
     for (size_t i = 0; i < n; i++) det->stage_events.push_back((cudaEvent_t)events[i]);
+    return ATAG_OK;
+}
+
+atag_status atag_detector_get_tuning(const atag_detector* det, atag_tuning* out) {
+    if (!det || !out) return fail(ATAG_ERR_INVALID_ARGUMENT, "get_tuning: null argument");
+    *out = det->tuning;
+    return ATAG_OK;
+}
+
+atag_status atag_detector_set_tuning(atag_detector* det, const atag_tuning* t) {
+    if (!det || !t) return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: null argument");
+    if ((t->ccl_tile_rows != 8 && t->ccl_tile_rows != 16) || (t->boundary_tile_rows != 8 && t->boundary_tile_rows != 16))
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: tile rows must be 8 or 16");
+    if (t->small_cluster_max < 1 || t->small_cluster_max > (int32_t)CF_SMALL_CAP)
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: small_cluster_max must be in [1, %u]", CF_SMALL_CAP);
+    if (t->small_ctas_per_sm < 1 || t->small_ctas_per_sm > 16 || t->large_ctas_divisor < 1 ||
+        t->large_ctas_divisor > 64 || t->index_ctas_per_sm < 1 || t->index_ctas_per_sm > 64)
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: CTA counts out of range");
+    det->tuning = *t;
     return ATAG_OK;
 }
 

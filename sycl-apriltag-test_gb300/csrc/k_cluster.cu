@@ -52,10 +52,9 @@ __global__ void __launch_bounds__(256) k_reset_frames(const __grid_constant__ Fr
 // ---------------------------------------------------------------------------
 // 1. boundaries + per-pair aggregation
 // ---------------------------------------------------------------------------
-constexpr int BP_W = 64, BP_H = 16;            // pixels per CTA tile
-constexpr int BP_SW = BP_W + 2, BP_SH = BP_H + 1;
+constexpr int BP_W = 64;                       // tile width; BP_H (8 or 16) rows is a tuning choice
+constexpr int BP_SW = BP_W + 2;
 constexpr int BP_LC = 256;                     // CTA hash-table entries
-constexpr int BP_THREADS = 256;                // 4 pixels per thread
 
 struct PairTableSmem {
     unsigned long long key[BP_LC];
@@ -117,7 +116,6 @@ __device__ __forceinline__ uint32_t global_flush(const FrameDesc& F, uint32_t gs
 
 // A staged point: CTA table slot (8 bits), tile-relative x (6) and y (4),
 // neighbour test (2) and colour direction (1).
-constexpr int BP_STAGE = BP_W * BP_H * 4;  // at most 4 points per pixel
 constexpr uint32_t STAGE_DIRECT = 1u << 21; // point already accounted for in global memory
 __device__ __forceinline__ uint32_t stage_entry(int ls, int xo, int yo, int t, int dir) {
     return ((uint32_t)ls << 13) | (uint32_t)xo | ((uint32_t)yo << 6) | ((uint32_t)t << 10) | ((uint32_t)dir << 12);
@@ -129,8 +127,10 @@ __device__ __forceinline__ uint32_t stage_packed(uint32_t e, uint32_t x0, uint32
 
 // find_boundaries (find_boundaries.cpp:10-155) fused with the per-pair
 // ClusterBounds reduction (main.cpp:571-585) and the compaction of points.
-__global__ void __launch_bounds__(BP_THREADS) k_boundaries_pairs(const __grid_constant__ FrameSet fs,
-                                                                 uint32_t min_size) {
+template <int BP_H>
+__device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32_t min_size) {
+    constexpr int BP_SH = BP_H + 1;
+    constexpr int BP_STAGE = BP_W * BP_H * 4;  // at most 4 points per pixel
     const FrameDesc& F = fs.get(blockIdx.y);
     const int w = F.width, h = F.height;
     const int ntx = (w + BP_W - 1) / BP_W, nty = (h + BP_H - 1) / BP_H;
@@ -305,7 +305,7 @@ constexpr int PF_THREADS = 1024;
 constexpr int PF_SMEM_KEYS = 6144;
 
 __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_constant__ FrameSet fs,
-                                                               PipelineParams p) {
+                                                               PipelineParams p, uint32_t small_max) {
     const FrameDesc& F = fs.get(blockIdx.x);
     uint32_t* status = F.counters + CNT_STATUS;
     __shared__ unsigned long long s_keys[PF_SMEM_KEYS];
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
         uint32_t cid = carry_cluster + block_exclusive_scan_u32(keep ? 1u : 0u, red, &tot_keep);
         uint32_t fstart = carry_fstart + block_exclusive_scan_u32(keep ? cnt : 0u, red, &tot_fcnt);
         const bool fits = keep && cid < F.cluster_cap && (unsigned long long)fstart + cnt <= F.cpoint_cap;
-        const bool small = cnt <= CF_SMALL_CAP;
+        const bool small = cnt <= small_max;
         uint32_t js = carry_small + block_exclusive_scan_u32(fits && small ? 1u : 0u, red, &tot_small);
         uint32_t jl = carry_large + block_exclusive_scan_u32(fits && !small ? 1u : 0u, red, &tot_large);
         if (fits) F.cluster_work[small ? js : F.cluster_cap - 1 - jl] = cid;
@@ -737,6 +737,15 @@ __global__ void __launch_bounds__(1024) k_compact_quads(const __grid_constant__ 
         F.stats->n_quads = carry < F.quad_cap ? carry : F.quad_cap;
         F.stats->status = F.counters[CNT_STATUS];
     }
+}
+
+__global__ void __launch_bounds__(BP_W / 4 * 8) k_boundaries_pairs_r8(const __grid_constant__ FrameSet fs,
+                                                                       uint32_t min_size) {
+    boundaries_pairs_impl<8>(fs, min_size);
+}
+__global__ void __launch_bounds__(BP_W / 4 * 16) k_boundaries_pairs_r16(const __grid_constant__ FrameSet fs,
+                                                                        uint32_t min_size) {
+    boundaries_pairs_impl<16>(fs, min_size);
 }
 
 }  // namespace atag

@@ -120,8 +120,7 @@ __global__ void __launch_bounds__(256) k_threshold(const __grid_constant__ Frame
 // (2) links that cross tile borders are merged in global memory;
 // (3) final labels, and tile counts folded into the component root.
 // ---------------------------------------------------------------------------
-constexpr int CCL_BX = 32, CCL_BY = 16;  // blocks per tile (64 x 32 pixels)
-constexpr int CCL_THREADS = CCL_BX * CCL_BY;
+constexpr int CCL_BX = 32;  // blocks per tile row; CCL_BY (8 or 16) rows is a tuning choice
 constexpr uint32_t UF_FIND_CAP = 1u << 23;   // longest parent chain followed
 constexpr uint32_t UF_UNION_CAP = 1u << 12;  // retries of one contended union
 
@@ -194,12 +193,15 @@ __device__ __forceinline__ bool uf_union(Ptr par, uint32_t a, uint32_t b) {
 }
 
 __device__ __forceinline__ uint32_t ccl_tiles_x(uint32_t w) { return (w / 2 + CCL_BX - 1) / CCL_BX; }
+template <int CCL_BY>
 __device__ __forceinline__ uint32_t ccl_tiles_y(uint32_t h) { return (h / 2 + CCL_BY - 1) / CCL_BY; }
 
-__global__ void __launch_bounds__(CCL_THREADS) k_ccl_local(const __grid_constant__ FrameSet fs) {
+template <int CCL_BY>
+__device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
+    constexpr int CCL_THREADS = CCL_BX * CCL_BY;
     const FrameDesc& F = fs.get(blockIdx.y);
     const int w = F.width, h = F.height;
-    const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y(h);
+    const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y<CCL_BY>(h);
     if ((int)blockIdx.x >= ntx * nty) return;
     const int bx0 = (blockIdx.x % ntx) * CCL_BX, by0 = (blockIdx.x / ntx) * CCL_BY;
     const int x0 = bx0 * 2, y0 = by0 * 2;
@@ -265,12 +267,12 @@ __global__ void __launch_bounds__(CCL_THREADS) k_ccl_local(const __grid_constant
 
 // Merge the links that cross tile borders: P/Q/R of the tile's top row,
 // P/S of its left column and R (up-right) of its right column.
-constexpr int CCL_BORDER_PER_TILE = CCL_BX + 2 * (CCL_BY - 1);
-
-__global__ void __launch_bounds__(256) k_ccl_border(const __grid_constant__ FrameSet fs) {
+template <int CCL_BY>
+__device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
+    constexpr int CCL_BORDER_PER_TILE = CCL_BX + 2 * (CCL_BY - 1);
     const FrameDesc& F = fs.get(blockIdx.y);
     const int w = F.width, h = F.height;
-    const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y(h);
+    const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y<CCL_BY>(h);
     const int per_tile = CCL_BORDER_PER_TILE;
     const int total = ntx * nty * per_tile;
     volatile uint32_t* par = F.scratch;
@@ -377,5 +379,10 @@ __global__ void __launch_bounds__(256) k_boundaries_dense(const __grid_constant_
         }
     }
 }
+
+__global__ void __launch_bounds__(CCL_BX * 8) k_ccl_local_r8(const __grid_constant__ FrameSet fs) { ccl_local_impl<8>(fs); }
+__global__ void __launch_bounds__(CCL_BX * 16) k_ccl_local_r16(const __grid_constant__ FrameSet fs) { ccl_local_impl<16>(fs); }
+__global__ void __launch_bounds__(256) k_ccl_border_r8(const __grid_constant__ FrameSet fs) { ccl_border_impl<8>(fs); }
+__global__ void __launch_bounds__(256) k_ccl_border_r16(const __grid_constant__ FrameSet fs) { ccl_border_impl<16>(fs); }
 
 }  // namespace atag

@@ -77,9 +77,9 @@ extern "C" atag_status atag_image_segmentation_noalloc(const uint8_t* thr, uint3
     d.sizes = sizes;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t tiles = ((w / 2 + 31) / 32) * ((h / 2 + 15) / 16);
-    k_ccl_local<<<dim3((unsigned)tiles, 1), 512, 0, s>>>(fs);
+    k_ccl_local_r16<<<dim3((unsigned)tiles, 1), 512, 0, s>>>(fs);
     count_launch();
-    k_ccl_border<<<dim3((unsigned)((tiles * (32 + 2 * (16 - 1)) + 255) / 256), 1), 256, 0, s>>>(fs);
+    k_ccl_border_r16<<<dim3((unsigned)((tiles * (32 + 2 * (16 - 1)) + 255) / 256), 1), 256, 0, s>>>(fs);
     count_launch();
     const size_t blocks = (w / 2) * (h / 2);
     k_ccl_final<<<dim3((unsigned)std::min<size_t>((blocks + 255) / 256, 8192), 1), 256, 0, s>>>(fs);

@@ -116,3 +116,45 @@ def test_detect_4k_stress():
     res = oracle.detect(img)
     assert_detect_matches(views, quads, res)
     assert int(res["extents"]["count"].max()) > 12288  # exercises the global-memory sort
+
+
+def test_mixed_resolution_batch_matches_oracle_and_singles():
+    """A batch drawn like the 64-frame benchmark batch (sizes from 640x480 to
+    2592x1944, 0-60 fiducials, 0-1000 clutter shapes each) gives every frame
+    the same result as alone, and the oracle's."""
+    from atag import synth
+    from atag.detector import Detector
+    specs = synth.batch_specs(10, seed=4)
+    imgs = [synth.render(s, 500 + i) for i, s in enumerate(specs)]
+    det = Detector(2592, 1944, max_frames=len(imgs), max_total_pixels=sum(i.size for i in imgs))
+    quads, st = det.detect([torch.from_numpy(i).cuda() for i in imgs])
+    alone = Detector(2592, 1944)
+    for i, img in enumerate(imgs):
+        assert int(st[i]["status"]) == 0
+        q, s1 = alone.detect([torch.from_numpy(img).cuda()])
+        assert_quads_match(quads[i], q[0], tol=0.0)
+        if i < 3:
+            assert_quads_match(quads[i], oracle.detect(img)["quads"])
+
+
+def test_every_tuning_gives_identical_results_and_autotune_applies(tmp_path):
+    from atag import autotune
+    from atag.detector import Detector
+    imgs = [synth_frame("1080p", 1), synth_frame("vga", 2)]
+    frames = [torch.from_numpy(i).cuda() for i in imgs]
+    det = Detector(1920, 1080, max_frames=2, max_total_pixels=sum(i.size for i in imgs))
+    base, _ = det.detect(frames)
+    for t in ({"ccl_tile_rows": 8, "boundary_tile_rows": 8, "small_cluster_max": 1024, "small_ctas_per_sm": 2,
+               "large_ctas_divisor": 8, "index_ctas_per_sm": 4},
+              {"ccl_tile_rows": 16, "boundary_tile_rows": 8, "small_cluster_max": 2048, "small_ctas_per_sm": 6,
+               "large_ctas_divisor": 2, "index_ctas_per_sm": 16}):
+        det.set_tuning(**t)
+        q, st = det.detect(frames)
+        for a, b in zip(q, base):
+            assert a.tobytes() == b.tobytes()
+    cache = str(tmp_path / "tune.json")
+    out = autotune.autotune(det, frames, reps=2, passes=1, cache_path=cache)
+    assert out["ms"] <= out["default_ms"] * 1.05
+    det2 = Detector(1920, 1080, max_frames=2, max_total_pixels=sum(i.size for i in imgs))
+    assert autotune.apply_cached(det2, frames, cache)
+    assert det2.get_tuning() == out["tuning"]

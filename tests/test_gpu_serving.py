@@ -1,0 +1,39 @@
+"""Serving on the GPU: 8 simulated cameras (4 x 1280x720 @ 60 fps, 4 x
+1920x1080 @ 30 fps) with Poisson arrivals go through the continuous-batching
+server; every result must equal the result of detecting that frame alone."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def test_each_result_is_the_same_alone_and_in_the_mix():
+    from atag import serving, synth
+    from atag.detector import Detector
+    specs = [synth.FrameSpec(1280, 720, 20, (16, 200), 150, (0.5, 1.5), (2.0, 8.0))] * 4 + \
+            [synth.FrameSpec(1920, 1080, 40, (16, 300), 300, (0.5, 1.5), (2.0, 8.0))] * 4
+    cams = [[synth.render(s, 100 * c + k) for k in range(2)] for c, s in enumerate(specs)]
+    # results alone
+    alone = {}
+    det = Detector(1920, 1080)
+    for c, frames in enumerate(cams):
+        for k, f in enumerate(frames):
+            q, st = det.detect([torch.from_numpy(f).cuda()])
+            alone[(c, k)] = q[0]
+    slots = [serving.DetectorExecutor(1920, 1080, max_frames=8, max_total_pixels=8 * 1920 * 1080)
+             for _ in range(3)]
+    srv = serving.Server(slots)
+    rates = [60.0] * 4 + [30.0] * 4
+    res = serving.run_cameras(srv, cams, rates, duration_s=1.5, seed=3)
+    assert len(res) > 300
+    counters = {}
+    for r in res:
+        k = counters.get(r.camera, 0)
+        counters[r.camera] = k + 1
+        want = alone[(r.camera, k % 2)]
+        assert r.quads.tobytes() == want.tobytes(), (r.seq, r.camera)
+        assert int(r.stats["status"]) == 0
+    summ = serving.latency_summary(res, 1.5)
+    assert summ["p99_ms"] < 100.0
+    print(summ)
