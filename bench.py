@@ -29,6 +29,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "sycl-apriltag-test_gb300")
 sys.path.insert(0, PKG)
+from atag import replicas  # noqa: E402
 
 METRIC = "1080p frames/s + p99 ms, batched vs plain on 1 GB300 (corner err <=1e-3 px)"
 W, H = 1920, 1080
@@ -156,6 +157,39 @@ def ncu_traffic(stage):
     return d.get(stage)
 
 
+def plain_path(args, det1, frames, stream):
+    """Single-frame latency: one graph replay per frame, the L2 flushed by a
+    256 MB write before each frame."""
+    import torch
+    inp = torch.empty((H, W), dtype=torch.uint8, device="cuda")
+    inp.copy_(frames[0])
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            det1.enqueue([inp], stream=stream)
+    stream.synchronize()
+    g1 = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g1, stream=stream):
+        det1.enqueue([inp], stream=stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    lat = []
+    with torch.cuda.stream(stream):
+        for i in range(args.plain_frames + args.warmup):
+            inp.copy_(frames[i % len(frames)])
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            g1.replay()
+            b.record(stream)
+            b.synchronize()
+            if i >= args.warmup:
+                lat.append(a.elapsed_time(b))
+    lat.sort()
+    p50 = lat[len(lat) // 2]
+    p99 = lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
+    return {"frames_per_s": 1000.0 / statistics.mean(lat), "p50_ms": p50, "p99_ms": p99,
+            "mean_ms": statistics.mean(lat), "frames": len(lat), "l2": "flushed (256 MB write) before each frame"}
+
+
 def run_reference(args, rank):
     """The reference arm: the CPU restatement of the reference path on all
     host threads, each step a bounded sample of the same workload."""
@@ -217,7 +251,8 @@ def main():
     extra_n = args.mixed if world == 1 else 0
     with concurrent.futures.ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1),
                                                 mp_context=mp.get_context("spawn")) as pool:
-        host_frames = render_frames(n_render, 1000 + rank * 100000, pool)
+        # frame k of the job has seed 1000 + k; rank r holds frames r, r + world, ...
+        host_frames = list(pool.map(_render, [1000 + k for k in replicas.job_frames(n_render, world, rank)]))
         specs = mixed_specs(extra_n, 77) if extra_n else []
         mixed_frames = list(pool.map(_render_spec, [(sp, 5000 + i) for i, sp in enumerate(specs)]))
         cam_frames = []
@@ -285,11 +320,7 @@ def main():
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(e0.elapsed_time(e1), device="cuda")
     value = B * args.steps * world / (ms / 1000.0)
     stats = det.stats()
 
@@ -315,34 +346,7 @@ def main():
                 "traffic": (traffic * B if traffic is not None else None)}
 
     # --- plain single-frame path: latency per frame, L2 flushed in between
-    det1 = Detector(w, h, config=cfg)
-    inp = torch.empty((H, W), dtype=torch.uint8, device="cuda")
-    inp.copy_(frames[0])
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            det1.enqueue([inp], stream=stream)
-    stream.synchronize()
-    g1 = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g1, stream=stream):
-        det1.enqueue([inp], stream=stream)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    lat = []
-    with torch.cuda.stream(stream):
-        for i in range(args.plain_frames + args.warmup):
-            inp.copy_(frames[i % B])
-            flush.zero_()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            g1.replay()
-            b.record(stream)
-            b.synchronize()
-            if i >= args.warmup:
-                lat.append(a.elapsed_time(b))
-    lat.sort()
-    p50 = lat[len(lat) // 2]
-    p99 = lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
-    plain = {"frames_per_s": 1000.0 / statistics.mean(lat), "p50_ms": p50, "p99_ms": p99,
-             "mean_ms": statistics.mean(lat), "frames": len(lat), "l2": "flushed (256 MB write) before each frame"}
+    plain = plain_path(args, Detector(w, h, config=cfg), frames, stream) if args.plain_frames > 0 else None
 
     # --- e2e: public API, host buffers in and out
     pinned = [torch.from_numpy(f).pin_memory() for f in host_frames[:B]]
@@ -364,12 +368,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
-    dt = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([dt], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dt = float(t.item())
-    e2e = {"value": B * args.steps * world / dt, "unit": "frames/s", "h2d_bytes_per_step": B * W * H,
+    dt = replicas.max_over_ranks(time.perf_counter() - t0, device="cuda")
+    e2e ={"value": B * args.steps * world / dt, "unit": "frames/s", "h2d_bytes_per_step": B * W * H,
            "d2h_bytes_per_step": h_stats.numel() + h_quads.numel()}
 
     # --- mixed-resolution batch (64 frames, 640x480 .. 2592x1944), one graph
@@ -439,7 +439,7 @@ def main():
     serving_line = None
     if cam_frames:
         from atag import serving
-        slots = [serving.DetectorExecutor(W, H, max_frames=8, max_total_pixels=8 * W * H) for _ in range(3)]
+        slots = serving.executors_for_memory(W, H, 8, 8 * W * H, max_slots=3)
         srv = serving.Server(slots)
         rates = [60.0] * 4 + [30.0] * 4
         res = serving.run_cameras(srv, cam_frames, rates, duration_s=args.serving_seconds, seed=1)
@@ -473,7 +473,7 @@ def main():
                    "l2": "not flushed: a step's working set (~50 MB per frame) exceeds the 129 MB L2",
                    "parallelism": f"replicas x{world}"},
         "plain": plain,
-        "batched_vs_plain": value / world / plain["frames_per_s"],
+        "batched_vs_plain": value / world / plain["frames_per_s"] if plain else None,
         "mixed_batch": mixed,
         "refine": refine_line,
         "serving": serving_line,

@@ -106,6 +106,36 @@ def slots_for_memory(free_bytes, slot_bytes, fraction=0.5, max_slots=8):
     return int(max(1, min(max_slots, (free_bytes * fraction) // max(slot_bytes, 1))))
 
 
+def executor_bytes(max_width, max_height, max_frames, max_total_pixels, config=None, quad_capacity=256,
+                   src_factor=1):
+    """Device bytes one DetectorExecutor keeps resident: the detector's
+    workspace (atag_workspace_size), its quad and stats buffers and the
+    input staging buffer."""
+    import ctypes
+
+    from . import lib
+    from .records import FRAME_STATS, QUAD_CORNERS
+    L = lib.init()
+    cfg = config or lib.default_config()
+    size = ctypes.c_size_t()
+    lib.check(L.atag_workspace_size(ctypes.byref(cfg), max_width, max_height, max_frames, max_total_pixels,
+                                    ctypes.byref(size)), "atag_workspace_size")
+    return (size.value + max_total_pixels * src_factor * src_factor +
+            max_frames * (quad_capacity * QUAD_CORNERS.itemsize + FRAME_STATS.itemsize))
+
+
+def executors_for_memory(max_width, max_height, max_frames, max_total_pixels, config=None, quad_capacity=256,
+                         src_factor=1, fraction=0.5, max_slots=8):
+    """As many DetectorExecutors as fit in `fraction` of the device's free
+    memory (at most `max_slots`, at least one)."""
+    import torch
+    free, _ = torch.cuda.mem_get_info()
+    need = executor_bytes(max_width, max_height, max_frames, max_total_pixels, config, quad_capacity, src_factor)
+    n = slots_for_memory(free, need, fraction, max_slots)
+    return [DetectorExecutor(max_width, max_height, max_frames, max_total_pixels, config, quad_capacity, src_factor)
+            for _ in range(n)]
+
+
 class Server:
     """Continuous batching over a pool of executors (slots)."""
 

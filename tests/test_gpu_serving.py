@@ -21,8 +21,8 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
         for k, f in enumerate(frames):
             q, st = det.detect([torch.from_numpy(f).cuda()])
             alone[(c, k)] = q[0]
-    slots = [serving.DetectorExecutor(1920, 1080, max_frames=8, max_total_pixels=8 * 1920 * 1080)
-             for _ in range(3)]
+    slots = serving.executors_for_memory(1920, 1080, 8, 8 * 1920 * 1080, max_slots=3)
+    assert len(slots) == 3
     srv = serving.Server(slots)
     rates = [60.0] * 4 + [30.0] * 4
     res = serving.run_cameras(srv, cams, rates, duration_s=1.5, seed=3)
