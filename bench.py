@@ -134,7 +134,8 @@ def stage_bytes(stats, n_src_px):
         "boundaries_pairs": 4 * N + 4 * N + 8 * P,  # labels, size gathers, tagged points
         "pairs_finalize": 48 * C,
         "scatter_points": 8 * P + 8 * Pf,
-        "cluster_fit": (8 + 4 + 8 + 64 + 2 * 64) * Pf,  # keys, grey taps, points, prefix sums, window ends
+        "cluster_sort": (8 + 4 + 8 + 64) * Pf,  # keys, grey taps, ClusterPoints, prefix sums
+        "cluster_errors": 48 * Pf,              # each prefix sum read once
         "index_quads": Cp * (120 + 210 * 8 * 48 + 272),
     }
 

@@ -358,9 +358,9 @@ typedef struct atag_tuning {
     int32_t boundary_tile_rows;   /* 8 or 16 pixel rows per boundary tile (16)      */
     int32_t small_cluster_max;    /* clusters up to this size use the 128-thread
                                      kernel, larger ones the 512-thread one
-                                     (1..4096, default 4096)                        */
-    int32_t small_ctas_per_sm;    /* persistent CTAs of the small-cluster kernel (4) */
-    int32_t large_ctas_divisor;   /* large-cluster CTAs = SMs / divisor (4)         */
+                                     (1..2048, default 2048)                        */
+    int32_t small_ctas_per_sm;    /* persistent CTAs of the small-cluster kernel (8) */
+    int32_t large_ctas_divisor;   /* large-cluster CTAs = SMs / divisor (2)         */
     int32_t index_ctas_per_sm;    /* CTAs of the combination search per SM (8)      */
 } atag_tuning;
 
@@ -372,7 +372,7 @@ atag_status atag_detector_set_tuning(atag_detector *det, const atag_tuning *tuni
  * after the last, so cudaEventElapsedTime(events[i], events[i+1]) is stage
  * i's device time.  Pass NULL / 0 to stop.  The reference prints cumulative
  * per-stage wall times instead (src/main.cpp:330-977). */
-#define ATAG_STAGE_COUNT 13
+#define ATAG_STAGE_COUNT 15
 atag_status atag_detector_set_stage_events(atag_detector *det, void *const *events, size_t n_events);
 /* Name of stage i (e.g. "ccl_local"), or NULL past the last. */
 const char *atag_stage_name(int stage);

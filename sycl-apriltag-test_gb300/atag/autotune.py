@@ -16,9 +16,9 @@ import statistics
 SPACE = {
     "ccl_tile_rows": [8, 16],
     "boundary_tile_rows": [8, 16],
-    "small_cluster_max": [1024, 2048, 4096],
-    "small_ctas_per_sm": [2, 4, 6],
-    "large_ctas_divisor": [2, 4, 8],
+    "small_cluster_max": [512, 1024, 2048],
+    "small_ctas_per_sm": [4, 8, 12],
+    "large_ctas_divisor": [1, 2, 4],
     "index_ctas_per_sm": [4, 8, 16],
 }
 

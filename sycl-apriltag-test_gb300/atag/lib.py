@@ -52,7 +52,7 @@ _SIGNATURES = {
     "atag_refine_forward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P]),
     "atag_refine_backward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P, _P, _P]),
 }
-STAGE_COUNT = 13
+STAGE_COUNT = 15
 
 _lib = None
 

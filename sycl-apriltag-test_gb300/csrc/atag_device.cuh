@@ -34,11 +34,148 @@ __host__ __device__ __forceinline__ long long wsub(long long a, long long b) {
     return (long long)((unsigned long long)a - (unsigned long long)b);
 }
 
-// hypotf as sqrt of the exactly-formed squares summed in double, rounded
-// once to float.
-__device__ __forceinline__ float hypot_f(float a, float b) {
+// ---------------------------------------------------------------------------
+// hypotf of the reference's host library: the squares formed exactly in
+// double, summed with one rounding to 53 bits, the square root rounded to 53
+// bits and then to float: R24(sqrt(R53(a^2 + b^2))) (the second rounding of
+// the root is innocuous: 53 >= 2*24 + 2).  FP64 runs at a small fraction of
+// the FP32/INT32 rate on this GPU, so the same roundings are carried out in
+// integer arithmetic:
+//   * |a| >= |b| = m_a 2^e_a, m_b 2^e_b with 24-bit integer significands;
+//   * a^2 + b^2 = (m_a^2 2^d + m_b^2) 2^(2 e_b), d = 2 (e_a - e_b), formed
+//     exactly in two 64-bit words (d < 56; for d >= 56, m_b^2 lies below the
+//     53-bit rounding position of m_a^2 2^d and the result is |a|);
+//   * rounded to a 53-bit significand M (to nearest, ties to even);
+//   * M scaled by an even power of two into [2^60, 2^62), its integer square
+//     root r (31 bits, Newton's method from a float estimate, then exact
+//     correction) and the remainder M - r^2 decide the rounding of r to 24
+//     bits (a remainder of 0 at the half-way point is a tie, to even).
+// Subnormal, huge (>= 2^63) and non-finite inputs never occur on the path;
+// they take the FP64 route.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint32_t f2u(float f) {
+#ifdef __CUDA_ARCH__
+    return __float_as_uint(f);
+#else
+    uint32_t u;
+    __builtin_memcpy(&u, &f, 4);
+    return u;
+#endif
+}
+__host__ __device__ __forceinline__ float u2f(uint32_t u) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(u);
+#else
+    float f;
+    __builtin_memcpy(&f, &u, 4);
+    return f;
+#endif
+}
+__host__ __device__ __forceinline__ int clz64(unsigned long long v) {
+#ifdef __CUDA_ARCH__
+    return __clzll((long long)v);
+#else
+    return v ? __builtin_clzll(v) : 64;
+#endif
+}
+__host__ __device__ __forceinline__ float hypot_f_fp64(float a, float b) {
+#ifdef __CUDA_ARCH__
     double da = (double)a, db = (double)b;
     return __double2float_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(da, da), __dmul_rn(db, db))));
+#else
+    const double da = (double)a, db = (double)b;
+    volatile double p = da * da, q = db * db;  // exact squares, no contraction
+    volatile double s = p + q;
+    return (float)__builtin_sqrt(s);
+#endif
+}
+// floor(sqrt(m)) for m in [2^60, 2^62), with 32-bit conversions only (the
+// 64-bit ones issue on the FP64 pipe): a float estimate from the top 32
+// bits (relative error < 2^-22, so within 2^10 of the root), one Newton
+// step on the exact integer residual, then exact +-1 correction.
+__host__ __device__ __forceinline__ unsigned long long isqrt_2_60(unsigned long long m) {
+    const uint32_t mh = (uint32_t)(m >> 30);  // [2^30, 2^32)
+    const uint32_t r0 = (uint32_t)(sqrtf((float)mh) * 32768.0f);
+    const long long e = (long long)(m - (unsigned long long)r0 * r0);
+    const float ef = (float)(int)(e >> 20) * 1048576.0f + (float)(uint32_t)(e & 0xFFFFF);
+    const int d = (int)rintf(ef / (2.0f * (float)r0));
+    unsigned long long u = (unsigned long long)((long long)r0 + d);
+    while (u * u > m) u--;
+    while ((u + 1) * (u + 1) <= m) u++;
+    return u;
+}
+__host__ __device__ __forceinline__ float u64_to_f32_rn(unsigned long long u) {
+    if (u < (1ull << 24)) return (float)(uint32_t)u;
+    const int L = 64 - clz64(u), sh = L - 24;  // sh >= 1
+    unsigned long long m = u >> sh;
+    const unsigned long long rem = u & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    int e = sh;
+    if (rem > half || (rem == half && (m & 1ull))) {
+        m++;
+        if (m >> 24) {
+            m >>= 1;
+            e++;
+        }
+    }
+    return u2f((uint32_t)(e + 23 + 127) << 23 | ((uint32_t)m & 0x7FFFFFu));
+}
+__host__ __device__ __forceinline__ float i64_to_f32_rn(long long v) {
+    const unsigned long long u = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+    const float f = u64_to_f32_rn(u);
+    return v < 0 ? -f : f;
+}
+__host__ __device__ __forceinline__ float hypot_f(float a, float b) {
+    uint32_t x = f2u(a) & 0x7FFFFFFFu, y = f2u(b) & 0x7FFFFFFFu;
+    if (x < y) {
+        const uint32_t t = x;
+        x = y;
+        y = t;
+    }
+    if (y == 0) return u2f(x);
+    if (x < 0x00800000u || x >= 0x5F000000u) return hypot_f_fp64(a, b);
+    const int ex = (int)(x >> 23) - 150;
+    const int ey = (y >> 23) ? (int)(y >> 23) - 150 : -149;
+    const unsigned long long mx = (x & 0x7FFFFFu) | 0x800000u;
+    const unsigned long long my = (y >> 23) ? ((y & 0x7FFFFFu) | 0x800000u) : (y & 0x7FFFFFu);
+    const int d = 2 * (ex - ey);
+    if (d >= 56) return u2f(x);
+    // S = hi:lo = mx^2 2^d + my^2, in units of 2^(2 ey)
+    const unsigned long long A = mx * mx, B = my * my;
+    unsigned long long lo = (A << d) + B;
+    unsigned long long hi = (d ? (A >> (64 - d)) : 0ull) + (lo < B ? 1ull : 0ull);
+    int E = 2 * ey;
+    const int L = hi ? 128 - clz64(hi) : 64 - clz64(lo);
+    unsigned long long M;
+    if (L <= 53) {
+        M = lo;
+    } else {
+        const int sh = L - 53;  // 1..50
+        M = (lo >> sh) | (hi << (64 - sh));
+        const unsigned long long rem = lo & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+        E += sh;
+        if (rem > half || (rem == half && (M & 1ull))) {
+            M++;
+            if (M >> 53) {
+                M >>= 1;
+                E++;
+            }
+        }
+    }
+    // M 2^E, M < 2^53: scale into [2^60, 2^62) with an even exponent
+    int s = 62 - (64 - clz64(M));
+    if ((E - s) & 1) s--;
+    const unsigned long long Mn = M << s;
+    E -= s;
+    const unsigned long long r = isqrt_2_60(Mn);  // [2^30, 2^31)
+    unsigned long long q = r >> 7;
+    const uint32_t low = (uint32_t)(r & 127u);
+    if (low > 64u || (low == 64u && (r * r != Mn || (q & 1ull)))) q++;
+    int k = E / 2 + 7;  // value = q 2^k
+    if (q >> 24) {
+        q >>= 1;
+        k++;
+    }
+    return u2f((uint32_t)(k + 23 + 127) << 23 | ((uint32_t)q & 0x7FFFFFu));
 }
 
 // ---------------------------------------------------------------------------
@@ -84,7 +221,7 @@ __device__ __forceinline__ float bounds_dot(uint32_t xmin, uint32_t xmax, uint32
     float cxcy = __double2float_rn(__dmul_rn((double)t, 0.5));
     float gxc = __double2float_rn(__dmul_rn(0.05118, (double)__int2float_rn(gx_sum)));
     float gyc = __double2float_rn(__dmul_rn(-0.028581, (double)__int2float_rn(gy_sum)));
-    float r = __fmul_rn(2.0f, __ll2float_rn(pxgx));
+    float r = __fmul_rn(2.0f, i64_to_f32_rn(pxgx));
     r = __fsub_rn(r, cxcy);
     r = __fsub_rn(r, gxc);
     r = __fsub_rn(r, gyc);
@@ -213,23 +350,24 @@ __device__ __forceinline__ void fit_line(const Moment& m, unsigned long long num
     long long Csxy = wsub(wmul(m.Mxy, m.W), wmul(m.Mx, m.My));
     long long Csyy = wsub(wmul(m.Myy, m.W), wmul(m.My, m.My));
     long long cf = wmul(wmul(m.W, m.W), 4);
-    float sdist = hypot_f(__ll2float_rn(wsub(Csxx, Csyy)), __ll2float_rn(wmul(2, Csxy)));
-    float num = __fsub_rn(__ll2float_rn(wadd(Csxx, Csyy)), sdist);
-    float eig = __fdiv_rn(num, __ll2float_rn(wmul(cf, 2)));
+    const float dxy = i64_to_f32_rn(wsub(Csxx, Csyy)), cxy2 = i64_to_f32_rn(wmul(2, Csxy));
+    float sdist = hypot_f(dxy, cxy2);
+    float num = __fsub_rn(i64_to_f32_rn(wadd(Csxx, Csyy)), sdist);
+    float eig = __fdiv_rn(num, i64_to_f32_rn(wmul(cf, 2)));
     if (lp) {
-        float nx1 = __fsub_rn(__ll2float_rn(wsub(Csxx, Csyy)), sdist);
-        float ny1 = __ll2float_rn(wmul(2, Csxy));
+        float nx1 = __fsub_rn(dxy, sdist);
+        float ny1 = cxy2;
         float nx2 = ny1;
-        float ny2 = __fsub_rn(__ll2float_rn(wsub(Csyy, Csxx)), sdist);
+        float ny2 = __fsub_rn(i64_to_f32_rn(wsub(Csyy, Csxx)), sdist);
         float M1 = __fadd_rn(__fmul_rn(nx1, nx1), __fmul_rn(ny1, ny1));
         float M2 = __fadd_rn(__fmul_rn(nx2, nx2), __fmul_rn(ny2, ny2));
         float nx, ny;
         if (M1 > M2) { nx = nx1; ny = ny1; } else { nx = nx2; ny = ny2; }
-        float w2 = __ll2float_rn(wmul(m.W, 2));
-        lp[0] = __fdiv_rn(__ll2float_rn(m.Mx), w2);
-        lp[1] = __fdiv_rn(__ll2float_rn(m.My), w2);
+        float w2 = i64_to_f32_rn(wmul(m.W, 2));
+        lp[0] = __fdiv_rn(i64_to_f32_rn(m.Mx), w2);
+        lp[1] = __fdiv_rn(i64_to_f32_rn(m.My), w2);
         float length = hypot_f(nx, ny);
-        if ((double)fabsf(length) < 1e-12) {
+        if (fabsf(length) < 0x1.19799ap-40f) {  // (double)|length| < 1e-12, in float
             lp[2] = 0.0f;
             lp[3] = 0.0f;
         } else {
@@ -237,7 +375,7 @@ __device__ __forceinline__ void fit_line(const Moment& m, unsigned long long num
             lp[3] = __fdiv_rn(ny, length);
         }
     }
-    if (err) *err = __fmul_rn(__ull2float_rn(num_in_moment), eig);
+    if (err) *err = __fmul_rn(u64_to_f32_rn(num_in_moment), eig);
     if (mse) *mse = eig;
 }
 
@@ -322,24 +460,27 @@ __device__ __forceinline__ float float_from_order_key(uint32_t k) {
 // the network, where every comparator points upward, so a missing partner
 // beyond n behaves as +infinity and is simply skipped.
 __device__ __forceinline__ void bitonic_sort_u64(unsigned long long* keys, uint32_t n) {
-    uint32_t npow = 1;
-    while (npow < n) npow <<= 1;
-    for (uint32_t k = 2; k <= npow; k <<= 1) {
-        // flip step
+    uint32_t npow = 1, lg = 0;
+    while (npow < n) {
+        npow <<= 1;
+        lg++;
+    }
+    for (uint32_t lk = 1; lk <= lg; lk++) {
+        // flip step of the merge of blocks of k = 2^lk
+        const uint32_t lh = lk - 1, hmask = (1u << lh) - 1u;
         for (uint32_t t = threadIdx.x; t < npow / 2; t += blockDim.x) {
-            uint32_t half = k >> 1;
-            uint32_t i = (t / half) * k + (t % half);
-            uint32_t j = (t / half) * k + (k - 1 - (t % half));
+            const uint32_t base = (t >> lh) << lk, r = t & hmask;
+            const uint32_t i = base + r, j = base + ((1u << lk) - 1u - r);
             if (j < n) {
                 unsigned long long a = keys[i], b = keys[j];
                 if (a > b) { keys[i] = b; keys[j] = a; }
             }
         }
         __syncthreads();
-        for (uint32_t j = k >> 2; j > 0; j >>= 1) {
+        for (int lj = (int)lk - 2; lj >= 0; lj--) {
+            const uint32_t jm = (1u << lj) - 1u;
             for (uint32_t t = threadIdx.x; t < npow / 2; t += blockDim.x) {
-                uint32_t i = (t / j) * (2 * j) + (t % j);
-                uint32_t p = i + j;
+                const uint32_t i = ((t >> lj) << (lj + 1)) + (t & jm), p = i + (1u << lj);
                 if (p < n) {
                     unsigned long long a = keys[i], b = keys[p];
                     if (a > b) { keys[i] = b; keys[p] = a; }
@@ -424,37 +565,151 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_u32(uint32_t v, uint32_
     return r;
 }
 
-// Stable LSD radix sort of n 64-bit keys, 8 bits per pass.  Each warp owns a
-// contiguous range of the input so the scatter keeps input order within a
-// digit.  `hist` holds (blockDim/32) x 256 counters, `red` 33 slots.
-// Passes where every key has the same digit are skipped.  Returns the
-// buffer that holds the sorted keys (a or b).
+// Stable LSD radix sort of n 64-bit keys for a CTA of THREADS threads, 8
+// bits per pass.  Each warp owns a contiguous range of the input so the
+// scatter keeps input order within a digit; passes where every key has the
+// same digit are skipped.  `hist` holds THREADS/32 x 256 counters, `red` 33
+// slots.  Returns the buffer that holds the sorted keys (a or b).  (Sorting
+// on the theta half alone and ordering ties afterwards does not pay: theta
+// carries a quadrant offset of 2^16, so it has 7 fractional bits there and
+// long runs of equal values.)
+// ---------------------------------------------------------------------------
+// Bitonic sort of T*K 64-bit keys held K per thread in registers.  On exit
+// thread t holds elements [t K, t K + K) of the ascending order.  Element e
+// lives in register e % K of thread e / K: compare distances below K are
+// register swaps, distances up to a warp are shuffles, longer ones go
+// through `xch` (T*K keys of shared memory, laid out r * T + t).
+// ---------------------------------------------------------------------------
+template <int K, int J>
+__device__ __forceinline__ void bitonic_regs_stage(unsigned long long (&v)[K], int base, int k) {
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+        if ((r ^ J) > r) {
+            const int p = r ^ J;
+            const bool asc = ((base + r) & k) == 0;
+            const unsigned long long a = v[r], b = v[p];
+            const bool sw = (a > b) == asc;
+            v[r] = sw ? b : a;
+            v[p] = sw ? a : b;
+        }
+    }
+}
+
+template <int T, int K>
+__device__ __forceinline__ void bitonic_sort_regs(unsigned long long (&v)[K], unsigned long long* xch) {
+    const int tid = threadIdx.x, base = tid * K;
+    for (int k = 2; k <= T * K; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= K) {
+                const int pj = j / K;
+                const bool keep_min = ((tid & pj) == 0) == ((tid & (k / K)) == 0);
+                if (pj < 32) {
+#pragma unroll
+                    for (int r = 0; r < K; r++) {
+                        const unsigned long long o = __shfl_xor_sync(0xFFFFFFFFu, v[r], pj);
+                        v[r] = keep_min ? (o < v[r] ? o : v[r]) : (o > v[r] ? o : v[r]);
+                    }
+                } else {
+                    __syncthreads();  // the previous exchange has been read
+#pragma unroll
+                    for (int r = 0; r < K; r++) xch[r * T + tid] = v[r];
+                    __syncthreads();
+#pragma unroll
+                    for (int r = 0; r < K; r++) {
+                        const unsigned long long o = xch[r * T + (tid ^ pj)];
+                        v[r] = keep_min ? (o < v[r] ? o : v[r]) : (o > v[r] ? o : v[r]);
+                    }
+                }
+            } else if (j == 1) {
+                bitonic_regs_stage<K, 1>(v, base, k);
+            } else if (j == 2) {
+                if constexpr (K > 2) bitonic_regs_stage<K, 2>(v, base, k);
+            } else if (j == 4) {
+                if constexpr (K > 4) bitonic_regs_stage<K, 4>(v, base, k);
+            } else if (j == 8) {
+                if constexpr (K > 8) bitonic_regs_stage<K, 8>(v, base, k);
+            } else if (j == 16) {
+                if constexpr (K > 16) bitonic_regs_stage<K, 16>(v, base, k);
+            }
+        }
+    }
+}
+
+// Sorts src[0, n) (global memory, n <= T*K) into dst[0, n) (shared memory of
+// T*K keys, also used for the exchange); all threads of the CTA call it.
+template <int T, int K>
+__device__ __forceinline__ void sort_keys_regs(const unsigned long long* __restrict__ src, uint32_t n,
+                                               unsigned long long* dst) {
+    static_assert(K <= 32 && (K & (K - 1)) == 0, "K must be a power of two up to 32");
+    unsigned long long v[K];
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+        const uint32_t e = (uint32_t)(r * T) + threadIdx.x;  // coalesced; the order is sorted away
+        v[r] = e < n ? src[e] : ~0ull;
+    }
+    bitonic_sort_regs<T, K>(v, dst);
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+        const uint32_t e = threadIdx.x * K + r;
+        if (e < n) dst[e] = v[r];
+    }
+    __syncthreads();
+}
+
+// Lanes of the warp whose 8-bit digit equals this lane's, among the lanes
+// with `valid` set: eight ballots (match.any on 32 distinct values is much
+// slower on this GPU).
+__device__ __forceinline__ unsigned match_digit8(uint32_t d, bool valid) {
+    unsigned m = __ballot_sync(0xFFFFFFFFu, valid);
+#pragma unroll
+    for (int b = 0; b < 8; b++) {
+        const bool bit = (d >> b) & 1u;
+        const unsigned bb = __ballot_sync(0xFFFFFFFFu, bit);
+        m &= bit ? bb : ~bb;
+    }
+    return m;
+}
+
+template <uint32_t THREADS>
 __device__ __forceinline__ unsigned long long* block_radix_sort_u64(unsigned long long* a, unsigned long long* b,
                                                                    uint32_t n, uint32_t* hist, uint32_t* red,
                                                                    uint32_t* s_flag) {
-    const uint32_t W = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr uint32_t W = THREADS / 32;
+    constexpr uint32_t PER = W * 256 / THREADS;  // scan entries per thread
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t lo = (uint32_t)((unsigned long long)n * w / W), hi = (uint32_t)((unsigned long long)n * (w + 1) / W);
     for (int pass = 0; pass < 8; pass++) {
         const int sh = pass * 8;
         __syncthreads();  // every thread is done with the previous pass's flag and counters
-        for (uint32_t i = threadIdx.x; i < W * 256; i += blockDim.x) hist[i] = 0;
+        for (uint32_t i = threadIdx.x; i < W * 256; i += THREADS) hist[i] = 0;
         if (threadIdx.x == 0) *s_flag = 0;
         __syncthreads();
-        for (uint32_t i = lo + lane; i < hi; i += 32) atomicAdd(&hist[w * 256 + (uint32_t)((a[i] >> sh) & 255)], 1u);
+        // warp-aggregated counts: lanes with equal digits add once (keys of
+        // one cluster share their high digits, which would serialise)
+        for (uint32_t base = lo; base < hi; base += 32) {
+            const uint32_t i = base + lane;
+            const bool v = i < hi;
+            const uint32_t d = v ? (uint32_t)((a[i] >> sh) & 255) : 0u;
+            const unsigned m = match_digit8(d, v);
+            if (v && (int)lane == __ffs(m) - 1) hist[w * 256 + d] += (uint32_t)__popc(m);
+            __syncwarp();
+        }
         __syncthreads();
-        if (threadIdx.x < 256) {
+        for (uint32_t d = threadIdx.x; d < 256; d += THREADS) {
             uint32_t t = 0;
-            for (uint32_t ww = 0; ww < W; ww++) t += hist[ww * 256 + threadIdx.x];
+#pragma unroll
+            for (uint32_t ww = 0; ww < W; ww++) t += hist[ww * 256 + d];
             if (t == n) *s_flag = 1;  // all keys share this digit: the pass is the identity
         }
         __syncthreads();
         if (*s_flag) continue;
-        // exclusive scan in (digit, warp) order; 8 consecutive entries per thread
-        uint32_t vals[8], sum = 0;
-        const uint32_t L0 = threadIdx.x * 8;
+        // exclusive scan in (digit, warp) order; PER consecutive entries per thread
+        uint32_t vals[PER], sum = 0;
+        const uint32_t L0 = threadIdx.x * PER;
 #pragma unroll
-        for (int e = 0; e < 8; e++) {
-            uint32_t L = L0 + e, d = L / W, ww = L % W;
+        for (uint32_t e = 0; e < PER; e++) {
+            const uint32_t L = L0 + e, d = L / W, ww = L % W;
             vals[e] = hist[ww * 256 + d];
             sum += vals[e];
         }
@@ -462,8 +717,8 @@ __device__ __forceinline__ unsigned long long* block_radix_sort_u64(unsigned lon
         uint32_t run = block_exclusive_scan_u32(sum, red, &total);
         __syncthreads();
 #pragma unroll
-        for (int e = 0; e < 8; e++) {
-            uint32_t L = L0 + e, d = L / W, ww = L % W;
+        for (uint32_t e = 0; e < PER; e++) {
+            const uint32_t L = L0 + e, d = L / W, ww = L % W;
             hist[ww * 256 + d] = run;
             run += vals[e];
         }
@@ -472,8 +727,8 @@ __device__ __forceinline__ unsigned long long* block_radix_sort_u64(unsigned lon
             const uint32_t i = base + lane;
             const bool v = i < hi;
             const unsigned long long key = v ? a[i] : 0ull;
-            const uint32_t d = v ? (uint32_t)((key >> sh) & 255) : 256u;
-            const unsigned m = __match_any_sync(0xffffffffu, d);
+            const uint32_t d = (uint32_t)((key >> sh) & 255);
+            const unsigned m = match_digit8(d, v);
             const uint32_t rank = __popc(m & ((1u << lane) - 1u));
             const uint32_t p = v ? hist[w * 256 + d] : 0u;
             __syncwarp();

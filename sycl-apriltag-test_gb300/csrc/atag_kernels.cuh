@@ -57,6 +57,7 @@ struct FrameDesc {
     atag_line_fit_point* line_fit;
     float* errbuf;                     // 2 floats per point (big clusters)
     uint32_t* cluster_work;            // small clusters from the front, large from the back
+    uint32_t* cluster_runs;            // first run (CE_RUN points) of each cluster
     // outputs
     atag_quad_corners* quads;
     uint32_t quad_cap;
@@ -84,17 +85,29 @@ enum Counter : uint32_t {
                          // known to exceed the cluster size limit are skipped)
     CNT_SMALL = 6,       // clusters of at most CF_SMALL_CAP points
     CNT_LARGE = 7,       // larger clusters
-    CNT_COUNT = 8
+    CNT_RUNS = 8,        // runs of up to CE_RUN points of one cluster
+    CNT_COUNT = 9
 };
 
-// Cluster-fit kernel shapes: most clusters are small and run several per SM
-// (bitonic sort in 32 KB of shared memory); large ones get a 512-thread CTA
-// with two 96 KB key buffers for a radix sort plus its histograms.  Larger
-// clusters than CF_LARGE_CAP sort in global memory.
-constexpr uint32_t CF_SMALL_THREADS = 128, CF_SMALL_CAP = 4096;
-constexpr uint32_t CF_LARGE_THREADS = 512, CF_LARGE_CAP = 12288;
+// Cluster-sort kernel shapes: most clusters are small and run several per SM
+// on 128 threads (up to 16 keys per thread), large ones get a 512-thread CTA
+// (up to 32 keys per thread); both sort in registers with a shared-memory
+// exchange buffer of CF_*_CAP keys.  Clusters larger than CF_LARGE_CAP (4K
+// frames only) radix-sort in global memory with per-warp counters.
+constexpr uint32_t CF_SMALL_THREADS = 128, CF_SMALL_CAP = CF_SMALL_THREADS * 16;
+constexpr uint32_t CF_LARGE_THREADS = 512, CF_LARGE_CAP = CF_LARGE_THREADS * 32;
 constexpr uint32_t CF_SMALL_SMEM = CF_SMALL_CAP * 8;
-constexpr uint32_t CF_LARGE_SMEM = 2 * CF_LARGE_CAP * 8 + (CF_LARGE_THREADS / 32) * 256 * 4;
+constexpr uint32_t CF_LARGE_SMEM = CF_LARGE_CAP * 8 + (CF_LARGE_THREADS / 32) * 256 * 4;
+// Window errors / filter / peaks: one warp per run of up to CE_RUN
+// consecutive points of one cluster.
+constexpr uint32_t CE_RUN = 256;
+
+// Batch-wide prefix offsets of up to four per-frame counters.
+struct BatchOffsets {
+    uint32_t which[4];
+    uint32_t* offsets[4];      // n_frames + 1 entries each, or null
+    uint32_t* work_counters;   // one queue cursor per used entry, reset to 0
+};
 
 struct PipelineParams {
     int min_white_black_diff;
@@ -136,13 +149,16 @@ __global__ void k_boundaries_pairs_r8(const __grid_constant__ FrameSet fs, uint3
 __global__ void k_boundaries_pairs_r16(const __grid_constant__ FrameSet fs, uint32_t min_size);
 __global__ void k_pairs_finalize(const __grid_constant__ FrameSet fs, PipelineParams p, uint32_t small_max);
 __global__ void k_scatter_points(const __grid_constant__ FrameSet fs);
-__global__ void k_cluster_fit_small(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets,
-                                    uint32_t n_frames, uint32_t* work_counter);
-__global__ void k_cluster_fit_large(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets,
-                                    uint32_t n_frames, uint32_t* work_counter);
+__global__ void k_cluster_sort_small(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets,
+                                     uint32_t n_frames, uint32_t* work_counter, uint32_t sort_cap);
+__global__ void k_cluster_sort_large(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets,
+                                     uint32_t n_frames, uint32_t* work_counter);
+__global__ void k_cluster_errors(const __grid_constant__ FrameSet fs, const uint32_t* run_offsets,
+                                 uint32_t n_frames, uint32_t* work_counter);
+__global__ void k_cluster_peaks(const __grid_constant__ FrameSet fs, const uint32_t* cluster_offsets,
+                                uint32_t n_frames);
 __global__ void k_peaks_scan(const __grid_constant__ FrameSet fs, PipelineParams p);
-__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, uint32_t which0,
-                                uint32_t* offsets0, uint32_t which1, uint32_t* offsets1, uint32_t* work_counters);
+__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, BatchOffsets a);
 __global__ void k_index_quads(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets, uint32_t n_frames,
                               PipelineParams p);
 __global__ void k_compact_quads(const __grid_constant__ FrameSet fs);

@@ -87,7 +87,7 @@ __device__ __forceinline__ int choose_combination(float err, uint32_t n, unsigne
     uint32_t lowest_key = block_min_u32(key, red32);
     float lowest = float_from_order_key(lowest_key);
     if (isinf(lowest) && lowest > 0) return -1;
-    bool q = (double)__fsub_rn(err, lowest) < 0.1;
+    bool q = __fsub_rn(err, lowest) < 0x1.99999ap-4f;  // (double)(err - lowest) < 0.1, in float
     uint32_t chosen = block_min_u32(q ? n : 0xFFFFFFFFu, red32);
     return chosen == 0xFFFFFFFFu ? -1 : (int)chosen;
 }

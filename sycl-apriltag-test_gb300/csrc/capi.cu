@@ -68,7 +68,8 @@ atag_status ensure_device(DeviceInfo** out) {
         cudaFuncAttributes fa;
         e = cudaFuncGetAttributes(&fa, k_threshold);
         if (e != cudaSuccess) return fail(ATAG_ERR_NO_DEVICE, "kernels do not load: %s", cudaGetErrorString(e));
-        CK(cudaFuncSetAttribute(k_cluster_fit_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF_LARGE_SMEM));
+        CK(cudaFuncSetAttribute(k_cluster_sort_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF_LARGE_SMEM));
+        CK(cudaFuncSetAttribute(k_cluster_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF_SMALL_SMEM));
         d.num_sms = prop.multiProcessorCount;
         d.smem_optin = prop.sharedMemPerBlockOptin;
         d.device = dev;
@@ -188,12 +189,14 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, FrameDe
     f.line_fit = (atag_line_fit_point*)take(sizeof(atag_line_fit_point) * c.cpoint_cap);
     f.errbuf = (float*)take(8ull * c.cpoint_cap);
     f.cluster_work = (uint32_t*)take(4ull * c.cluster_cap);
+    f.cluster_runs = (uint32_t*)take(4ull * c.cluster_cap);
     f.counters = (uint32_t*)take(4ull * CNT_COUNT);
     if (d) *d = f;
     return off;
 }
 
 constexpr int RING = 16;
+constexpr size_t WORK_LISTS = 5;  // batch-wide work lists of the per-cluster kernels
 
 }  // namespace
 
@@ -215,7 +218,7 @@ struct atag_detector {
     bool owns_ws = false;
     // header carve-out
     FrameDesc* d_tables = nullptr;   // RING x max_frames
-    uint32_t* d_work = nullptr;      // offsets (3 x (max_frames + 1)) + 3 counters
+    uint32_t* d_work = nullptr;      // offsets (WORK_LISTS x (max_frames + 1)) + WORK_LISTS counters
     cudaStream_t side = nullptr;     // second stream for the large-cluster kernel
     cudaEvent_t fork = nullptr, join = nullptr;
     uint8_t* d_input = nullptr;      // host-upload input region
@@ -233,7 +236,7 @@ struct atag_detector {
     std::vector<FrameDesc> last;     // table last uploaded
     std::vector<FrameDesc> cur;      // table of the last call
     std::vector<cudaEvent_t> stage_events;
-    atag_tuning tuning{16, 16, (int32_t)CF_SMALL_CAP, 4, 4, 8};
+    atag_tuning tuning{16, 16, (int32_t)CF_SMALL_CAP, 8, 2, 8};
 };
 
 namespace {
@@ -243,7 +246,7 @@ constexpr size_t HOST_QUAD_CAP = 4096;
 size_t header_bytes(size_t max_frames, size_t input_bytes) {
     size_t b = 0;
     b += al(sizeof(FrameDesc) * RING * max_frames);
-    b += al(4 * (3 * (max_frames + 1) + 3));
+    b += al(4 * (WORK_LISTS * (max_frames + 1) + WORK_LISTS));
     b += al(input_bytes);
     b += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
     b += al(sizeof(atag_frame_stats));
@@ -351,8 +354,8 @@ static atag_status launch_segmentation(const FrameSet& fs, size_t max_w, size_t 
         k_ccl_border_r16<<<grid2(cdiv(border, 256), nf), 256, 0, s>>>(fs);
         LAUNCHED();
     }
-    size_t blocks = (max_w / 2) * (max_h / 2);
-    k_ccl_final<<<grid2(std::min<size_t>(cdiv(blocks, 256), 8192), nf), 256, 0, s>>>(fs);
+    size_t pairs = (max_w / 4) * (max_h / 2);  // k_ccl_final takes two 2x2 blocks per thread
+    k_ccl_final<<<grid2(std::min<size_t>(cdiv(pairs, 256), 8192), nf), 256, 0, s>>>(fs);
     LAUNCHED();
     return ATAG_OK;
 }
@@ -479,7 +482,7 @@ atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t ma
     }
     char* p = det->ws;
     det->d_tables = (FrameDesc*)p; p += al(sizeof(FrameDesc) * RING * max_frames);
-    det->d_work = (uint32_t*)p; p += al(4 * (3 * (max_frames + 1) + 3));
+    det->d_work = (uint32_t*)p; p += al(4 * (WORK_LISTS * (max_frames + 1) + WORK_LISTS));
     det->input_bytes = max_total_pixels * (size_t)c.decimate * (size_t)c.decimate;
     det->d_input = (uint8_t*)p; p += al(det->input_bytes);
     det->d_hquads = (atag_quad_corners*)p; p += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
@@ -581,10 +584,14 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     fs.table = d_table;
     const PipelineParams& p = det->pp;
     const int sms = det->dev->num_sms;
+    // batch-wide work lists: small clusters, large clusters, point runs,
+    // all clusters, clusters with peaks; one queue cursor each
     uint32_t* off_small = det->d_work;
     uint32_t* off_large = det->d_work + (n + 1);
-    uint32_t* off_peaks = det->d_work + 2 * (n + 1);
-    uint32_t* wc = det->d_work + 3 * (det->max_frames + 1);
+    uint32_t* off_runs = det->d_work + 2 * (n + 1);
+    uint32_t* off_clusters = det->d_work + 3 * (n + 1);
+    uint32_t* off_peaks = det->d_work + 4 * (n + 1);
+    uint32_t* wc = det->d_work + WORK_LISTS * (det->max_frames + 1);
 
     const bool timed = det->stage_events.size() == ATAG_STAGE_COUNT + 1;
     auto mark = [&](int i) -> atag_status {
@@ -619,7 +626,7 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
         LAUNCHED();
     }
     STAGE(5);
-    k_ccl_final<<<grid2(std::min<size_t>(cdiv((mw / 2) * (mh / 2), 256), 8192), n), 256, 0, s>>>(fs);
+    k_ccl_final<<<grid2(std::min<size_t>(cdiv((mw / 4) * (mh / 2), 256), 8192), n), 256, 0, s>>>(fs);
     LAUNCHED();
     STAGE(6);
     if (bp_rows == 8)
@@ -630,7 +637,11 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     STAGE(7);
     k_pairs_finalize<<<(unsigned)n, 1024, 0, s>>>(fs, p, (uint32_t)tu.small_cluster_max);
     LAUNCHED();
-    k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_SMALL, off_small, CNT_LARGE, off_large, wc);
+    {
+        BatchOffsets bo{{CNT_SMALL, CNT_LARGE, CNT_RUNS, CNT_CLUSTERS},
+                        {off_small, off_large, off_runs, off_clusters}, wc};
+        k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, bo);
+    }
     LAUNCHED();
     STAGE(8);
     k_scatter_points<<<grid2(std::min<size_t>(cdiv(max_points, 256), 1024), n), 256, 0, s>>>(fs);
@@ -639,27 +650,40 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     // large clusters on the side stream, concurrently with the small ones
     CK(cudaEventRecord(det->fork, s));
     CK(cudaStreamWaitEvent(det->side, det->fork, 0));
-    k_cluster_fit_large<<<std::max(1, sms / std::max(1, tu.large_ctas_divisor)), CF_LARGE_THREADS, CF_LARGE_SMEM,
-                          det->side>>>(fs, off_large,
-                                                                                                (uint32_t)n, wc + 1);
+    k_cluster_sort_large<<<std::max(1, sms / std::max(1, tu.large_ctas_divisor)), CF_LARGE_THREADS, CF_LARGE_SMEM,
+                           det->side>>>(fs, off_large, (uint32_t)n, wc + 1);
     LAUNCHED();
-    k_cluster_fit_small<<<sms * std::max(1, tu.small_ctas_per_sm), CF_SMALL_THREADS, CF_SMALL_SMEM, s>>>(
-        fs, off_small, (uint32_t)n, wc);
+    {
+        // the small-cluster kernel's key buffers are sized for the tuned split
+        const uint32_t cap = (uint32_t)tu.small_cluster_max;
+        const uint32_t smem = cap * 8;
+        k_cluster_sort_small<<<sms * std::max(1, tu.small_ctas_per_sm), CF_SMALL_THREADS, smem, s>>>(
+            fs, off_small, (uint32_t)n, wc, cap);
+    }
     LAUNCHED();
     CK(cudaEventRecord(det->join, det->side));
     CK(cudaStreamWaitEvent(s, det->join, 0));
     STAGE(10);
-    k_peaks_scan<<<(unsigned)n, 1024, 0, s>>>(fs, p);
-    LAUNCHED();
-    k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, CNT_PEAKCLU, off_peaks, 0, nullptr, wc + 2);
+    k_cluster_errors<<<sms * 8, 256, 0, s>>>(fs, off_runs, (uint32_t)n, wc + 2);
     LAUNCHED();
     STAGE(11);
-    k_index_quads<<<sms * std::max(1, tu.index_ctas_per_sm), 256, 0, s>>>(fs, off_peaks, (uint32_t)n, p);
+    k_cluster_peaks<<<sms * 4, 256, 0, s>>>(fs, off_clusters, (uint32_t)n);
     LAUNCHED();
     STAGE(12);
-    k_compact_quads<<<(unsigned)n, 1024, 0, s>>>(fs);
+    k_peaks_scan<<<(unsigned)n, 1024, 0, s>>>(fs, p);
+    LAUNCHED();
+    {
+        BatchOffsets bo{{CNT_PEAKCLU, 0, 0, 0}, {off_peaks, nullptr, nullptr, nullptr}, wc + 4};
+        k_batch_offsets<<<1, 1024, 0, s>>>(fs, (uint32_t)n, bo);
+    }
     LAUNCHED();
     STAGE(13);
+    k_index_quads<<<sms * std::max(1, tu.index_ctas_per_sm), 256, 0, s>>>(fs, off_peaks, (uint32_t)n, p);
+    LAUNCHED();
+    STAGE(14);
+    k_compact_quads<<<(unsigned)n, 1024, 0, s>>>(fs);
+    LAUNCHED();
+    STAGE(15);
 #undef STAGE
     return ATAG_OK;
 }
@@ -749,7 +773,8 @@ atag_status atag_detector_set_tuning(atag_detector* det, const atag_tuning* t) {
 const char* atag_stage_name(int i) {
     static const char* names[ATAG_STAGE_COUNT] = {
         "reset", "decimate", "threshold", "ccl_local", "ccl_border", "ccl_final", "boundaries_pairs",
-        "pairs_finalize", "scatter_points", "cluster_fit", "peaks_scan", "index_quads", "compact_quads"};
+        "pairs_finalize", "scatter_points", "cluster_sort", "cluster_errors", "cluster_peaks", "peaks_scan",
+        "index_quads", "compact_quads"};
     return (i >= 0 && i < ATAG_STAGE_COUNT) ? names[i] : nullptr;
 }
 

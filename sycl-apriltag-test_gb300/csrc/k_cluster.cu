@@ -16,10 +16,11 @@
 //      each surviving pair its cluster index and extent;
 //   3. k_scatter_points: points of surviving pairs go straight into their
 //      cluster's segment with their theta key; the rest are dropped;
-//   4. k_cluster_fit: one CTA per cluster sorts by (theta, point) in shared
-//      memory and does line-fit moments, the prefix scan, the windowed
-//      errors, the 7-tap filter and the peak search (fit_lines), keeping
-//      the 10 best peaks;
+//   4. k_cluster_sort: one CTA per cluster sorts by (theta, point) in
+//      shared memory and writes ClusterPoints and the line-fit prefix sums;
+//      k_cluster_errors: fit_lines (windowed errors, 7-tap filter, peaks)
+//      flat over all cluster points; k_cluster_peaks: the 10 best peaks of
+//      each cluster;
 //   5. k_peaks_scan / k_index_quads / k_compact_quads: peak extents,
 //      do_indexing and the corner intersection, quads in reference order.
 #include "atag_kernels.cuh"
@@ -145,12 +146,26 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     __shared__ uint32_t red[33];
     __shared__ uint32_t s_base;
 
-    for (int i = threadIdx.x; i < BP_SH * BP_SW; i += blockDim.x) {
-        int r = i / BP_SW, c = i % BP_SW;
-        int y = y0 + r, x = x0 - 1 + c;
-        uint32_t l = (x >= 0 && x < w && y < h) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
-        lab[r][c] = l;
-        big[r][c] = __ldg(F.sizes + (l & LABEL_VALUE_MASK)) >= min_size;
+    // labels of the tile and its halo, then the size of each label's
+    // component: all label loads of a thread are issued before its size
+    // gathers, so the two dependent round trips overlap across iterations
+    {
+        constexpr int THREADS = BP_W / 4 * BP_H, NL = (BP_SH * BP_SW + THREADS - 1) / THREADS;
+        uint32_t lv[NL];
+#pragma unroll
+        for (int k = 0; k < NL; k++) {
+            const int i = threadIdx.x + k * THREADS, r = i / BP_SW, c = i % BP_SW;
+            const int y = y0 + r, x = x0 - 1 + c;
+            lv[k] = (i < BP_SH * BP_SW && x >= 0 && x < w && y < h) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < NL; k++) {
+            const int i = threadIdx.x + k * THREADS, r = i / BP_SW, c = i % BP_SW;
+            if (i < BP_SH * BP_SW) {
+                lab[r][c] = lv[k];
+                big[r][c] = __ldg(F.sizes + (lv[k] & LABEL_VALUE_MASK)) >= min_size;
+            }
+        }
     }
     for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
         T.key[i] = EMPTY_KEY;
@@ -332,7 +347,8 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
     fp.tag_width = p.tag_width;
     fp.normal_border = p.normal_border;
     fp.reversed_border = p.reversed_border;
-    uint32_t carry_start = 0, carry_cluster = 0, carry_fstart = 0, carry_small = 0, carry_large = 0;
+    uint32_t carry_start = 0, carry_cluster = 0, carry_fstart = 0, carry_small = 0, carry_large = 0, carry_fit = 0;
+    uint32_t carry_runs = 0;
     for (uint32_t c0 = 0; c0 < C; c0 += blockDim.x) {
         uint32_t c = c0 + threadIdx.x;
         uint32_t slot = INVALID, cnt = 0;
@@ -348,7 +364,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
             pxgx = (long long)F.pair_pxgx[slot];
             keep = valid_blob(fp, cnt, bb.x, bb.y, bb.z, bb.w, gs.x, gs.y, pxgx);
         }
-        uint32_t tot_cnt, tot_keep, tot_fcnt, tot_small, tot_large;
+        uint32_t tot_cnt, tot_keep, tot_fcnt, tot_small, tot_large, tot_fit, tot_runs;
         uint32_t start = carry_start + block_exclusive_scan_u32(cnt, red, &tot_cnt);
         uint32_t cid = carry_cluster + block_exclusive_scan_u32(keep ? 1u : 0u, red, &tot_keep);
         uint32_t fstart = carry_fstart + block_exclusive_scan_u32(keep ? cnt : 0u, red, &tot_fcnt);
@@ -356,6 +372,9 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
         const bool small = cnt <= small_max;
         uint32_t js = carry_small + block_exclusive_scan_u32(fits && small ? 1u : 0u, red, &tot_small);
         uint32_t jl = carry_large + block_exclusive_scan_u32(fits && !small ? 1u : 0u, red, &tot_large);
+        block_exclusive_scan_u32(fits ? cnt : 0u, red, &tot_fit);
+        const uint32_t run0 = carry_runs + block_exclusive_scan_u32(fits ? (cnt + CE_RUN - 1) / CE_RUN : 0u, red,
+                                                                    &tot_runs);
         if (fits) F.cluster_work[small ? js : F.cluster_cap - 1 - jl] = cid;
         if (keep) {
             if (!fits) {
@@ -374,6 +393,7 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
                 F.cluster_extents[cid] = atag_cluster_extents{fstart, cnt};
                 F.cluster_center[cid] = make_float2(bounds_cx(bb.x, bb.y), bounds_cy(bb.z, bb.w));
                 F.cluster_cursor[cid] = 0;
+                F.cluster_runs[cid] = run0;
                 F.peak_count[cid] = 0;
             }
         }
@@ -382,32 +402,35 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
         carry_fstart += tot_fcnt;
         carry_small += tot_small;
         carry_large += tot_large;
+        carry_fit += tot_fit;
+        carry_runs += tot_runs;
     }
     if (threadIdx.x == 0) {
-        uint32_t ncl = carry_cluster, npf = carry_fstart;
-        if (ncl > F.cluster_cap) ncl = F.cluster_cap;
-        // clusters are assigned in order, so the kept prefix is [0, ncl)
-        F.counters[CNT_CLUSTERS] = ncl;
+        // clusters are assigned in order and the capacity checks are
+        // monotone, so the clusters that fit are the prefix [0, nfit) and
+        // their points the prefix [0, carry_fit) of the cluster point array
+        const uint32_t nfit = carry_small + carry_large;
+        F.counters[CNT_CLUSTERS] = nfit;
         F.counters[CNT_SMALL] = carry_small;
         F.counters[CNT_LARGE] = carry_large;
+        F.counters[CNT_RUNS] = carry_runs;
         F.stats->width = F.width;
         F.stats->height = F.height;
         F.stats->n_points = F.counters[CNT_ALLPOINTS];
         F.stats->n_pairs = C;
-        F.stats->n_clusters = ncl;
-        F.stats->n_cluster_points = npf < F.cpoint_cap ? npf : F.cpoint_cap;
+        F.stats->n_clusters = nfit;
+        F.stats->n_cluster_points = carry_fit;
     }
 }
 
 // Prefix offsets of per-frame counts over the batch (the flattened work
 // spaces of the per-cluster kernels) and reset of their queue cursors.
-__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, uint32_t which0,
-                                uint32_t* __restrict__ offsets0, uint32_t which1, uint32_t* __restrict__ offsets1,
-                                uint32_t* __restrict__ work_counters) {
+__global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_frames, BatchOffsets a) {
     __shared__ uint32_t red[33];
-    for (int k = 0; k < 2; k++) {
-        uint32_t which = k ? which1 : which0;
-        uint32_t* offsets = k ? offsets1 : offsets0;
+    for (int k = 0; k < 4; k++) {
+        const uint32_t which = a.which[k];
+        uint32_t* offsets = a.offsets[k];
+        uint32_t* work_counters = a.work_counters;
         if (!offsets) continue;
         uint32_t carry = 0;
         for (uint32_t f0 = 0; f0 < n_frames; f0 += blockDim.x) {
@@ -459,7 +482,8 @@ __global__ void __launch_bounds__(256) k_scatter_points(const __grid_constant__ 
 }
 
 // ---------------------------------------------------------------------------
-// 4. one cluster per CTA: sort, moments, scan, errors, filter, peaks
+// 4. one cluster per CTA: sort by (theta, point), ClusterPoints, line-fit
+// inputs and their prefix sums
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ long long shfl_up_ll(long long v, int o) {
@@ -520,16 +544,44 @@ __device__ __forceinline__ uint32_t find_frame(const uint32_t* offsets, uint32_t
     return lo;
 }
 
+// Warp-wide inclusive scan of 6 int64 lanes (wrapping adds).
+__device__ __forceinline__ Moment warp_inclusive_scan_moment(Moment v) {
+    const int lane = threadIdx.x & 31;
+    long long x[6] = {v.Mx, v.My, v.Mxx, v.Myy, v.Mxy, v.W};
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+#pragma unroll
+        for (int j = 0; j < 6; j++) {
+            const long long y = shfl_up_ll(x[j], o);
+            if (lane >= o) x[j] = wadd(x[j], y);
+        }
+    }
+    return Moment{x[0], x[1], x[2], x[3], x[4], x[5]};
+}
+__device__ __forceinline__ Moment warp_sum_moment(Moment v) {
+    long long x[6] = {v.Mx, v.My, v.Mxx, v.Myy, v.Mxy, v.W};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int j = 0; j < 6; j++)
+            x[j] = wadd(x[j], (long long)__shfl_xor_sync(0xffffffffu, (unsigned long long)x[j], o));
+    return Moment{x[0], x[1], x[2], x[3], x[4], x[5]};
+}
+__device__ __forceinline__ Moment shfl_moment(const Moment& v, int src) {
+    auto s = [&](long long x) { return (long long)__shfl_sync(0xffffffffu, (unsigned long long)x, src); };
+    return Moment{s(v.Mx), s(v.My), s(v.Mxx), s(v.Myy), s(v.Mxy), s(v.W)};
+}
+
 template <bool LARGE>
-__device__ __forceinline__ void cluster_fit(const FrameSet& fs, const uint32_t* __restrict__ work_offsets,
-                                            uint32_t n_frames, uint32_t* __restrict__ work_counter) {
+__device__ __forceinline__ void cluster_sort(const FrameSet& fs, const uint32_t* __restrict__ work_offsets,
+                                             uint32_t n_frames, uint32_t* __restrict__ work_counter,
+                                             uint32_t sort_cap) {
+    constexpr uint32_t THREADS = LARGE ? CF_LARGE_THREADS : CF_SMALL_THREADS;
     extern __shared__ unsigned long long smem_keys[];
-    constexpr uint32_t sort_cap = LARGE ? CF_LARGE_CAP : CF_SMALL_CAP;
     __shared__ long long red_m[32][6];
-    __shared__ unsigned long long red64[32];
     __shared__ uint32_t red32[33];
-    __shared__ uint32_t s_item, s_ncand, s_flag;
-    uint32_t* hist = reinterpret_cast<uint32_t*>(smem_keys + 2 * sort_cap);
+    __shared__ uint32_t s_item, s_flag;
+    uint32_t* hist = reinterpret_cast<uint32_t*>(smem_keys + sort_cap);  // radix counters (global-memory sorts)
     const uint32_t total = work_offsets[n_frames];
     for (;;) {
         __syncthreads();
@@ -543,90 +595,227 @@ __device__ __forceinline__ void cluster_fit(const FrameSet& fs, const uint32_t* 
         const uint32_t cid = F.cluster_work[LARGE ? F.cluster_cap - 1 - j : j];
         const atag_cluster_extents ext = F.cluster_extents[cid];
         const uint32_t n = ext.count, start = ext.start;
-        const bool in_smem = n <= sort_cap;
-        unsigned long long* A = in_smem ? smem_keys : F.sortbuf + start;
-        if (in_smem)
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) A[i] = F.sortbuf[start + i];
-        __syncthreads();
         // sort by (theta, packed point): the reference's (cluster, slope)
-        // order (main.cpp:737-750) with ties fixed by the point
-        unsigned long long* X = A;
-        if (LARGE && n > 1024) {
-            unsigned long long* Bb = in_smem ? smem_keys + sort_cap
-                                             : reinterpret_cast<unsigned long long*>(F.errbuf + 2ull * start);
-            X = block_radix_sort_u64(A, Bb, n, hist, red32, &s_flag);
+        // order (main.cpp:737-750) with ties fixed by the point.  Up to
+        // sort_cap keys: a bitonic sort in registers sized to the cluster;
+        // larger clusters (4K frames only): radix sort in global memory.
+        unsigned long long* X = smem_keys;
+        const unsigned long long* src = F.sortbuf + start;
+        if (n <= sort_cap) {
+            if (LARGE) {
+                if (n <= THREADS * 8) sort_keys_regs<THREADS, 8>(src, n, X);
+                else if (n <= THREADS * 16) sort_keys_regs<THREADS, 16>(src, n, X);
+                else sort_keys_regs<THREADS, 32>(src, n, X);
+            } else {
+                if (n <= THREADS * 2) sort_keys_regs<THREADS, 2>(src, n, X);
+                else if (n <= THREADS * 4) sort_keys_regs<THREADS, 4>(src, n, X);
+                else if (n <= THREADS * 8) sort_keys_regs<THREADS, 8>(src, n, X);
+                else sort_keys_regs<THREADS, 16>(src, n, X);
+            }
         } else {
-            bitonic_sort_u64(A, n);
+            X = block_radix_sort_u64<THREADS>(F.sortbuf + start,
+                                              reinterpret_cast<unsigned long long*>(F.errbuf + 2ull * start), n,
+                                              hist, red32, &s_flag);
+            __syncthreads();
         }
-        __syncthreads();
         // ClusterPoints out; the key slot is reused for the line-fit inputs
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-            const unsigned long long k = X[i];
-            const uint32_t packed = (uint32_t)k;
-            atag_cluster_point cp;
-            cp.packed_x = (uint16_t)packed;
-            cp.packed_y = (uint16_t)(packed >> 16);
-            cp.slope = float_from_order_key((uint32_t)(k >> 32));
-            F.cluster_points[start + i] = cp;
-            X[i] = linefit_rxyw(packed, F.width, F.height, F.grey);
-        }
-        __syncthreads();
-        // segmented inclusive scan of the moments (main.cpp:796-801)
-        {
-            const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
-            const uint32_t i0 = min(n, threadIdx.x * per), i1 = min(n, i0 + per);
-            Moment tot{0, 0, 0, 0, 0, 0};
-            for (uint32_t i = i0; i < i1; i++) tot = m_add(tot, moment_of(X[i]));
-            Moment run = block_exclusive_scan_moment(tot, red_m);
-            for (uint32_t i = i0; i < i1; i++) {
-                run = m_add(run, moment_of(X[i]));
-                store_moment(F.line_fit + start + i, run);
-            }
-        }
-        __syncthreads();
-        // errors of the windows around each point, then the cyclic filter
-        float* err = reinterpret_cast<float*>(X);
-        float* flt = err + n;
-        const atag_line_fit_point* cpts = F.line_fit + start;
-        const uint32_t kwin = min(20u, n / 12);
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) err[i] = window_error_local(cpts, n, kwin, i);
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-            float acc = 0.0f;
+        // (four points per thread in flight, so their image reads overlap)
+        for (uint32_t i0 = threadIdx.x; i0 < n; i0 += 4 * blockDim.x) {
+            unsigned long long k[4];
 #pragma unroll
-            for (int j = 0; j < 7; j++) {
-                int t = (int)i + j - 3;
-                t = t < 0 ? t + (int)n : (t >= (int)n ? t - (int)n : t);
-                acc = __fadd_rn(acc, __fmul_rn(err[t], filter_tap(j)));
+            for (int u = 0; u < 4; u++) {
+                const uint32_t i = i0 + u * blockDim.x;
+                k[u] = i < n ? X[i] : 0ull;
             }
-            flt[i] = acc;
-        }
-        if (threadIdx.x == 0) s_ncand = 0;
-        __syncthreads();
-        // strict local maxima with error != 0 (D10), global point 0 excluded,
-        // compacted as (error, ~index) keys into the now free error array
-        unsigned long long* cand = reinterpret_cast<unsigned long long*>(err);
-        for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-            float cur = flt[i];
-            float prev = flt[i == 0 ? n - 1 : i - 1], next = flt[i + 1 == n ? 0 : i + 1];
-            if (cur > prev && cur > next && cur != 0.0f && !(cid == 0 && i == 0)) {
-                uint32_t pos = atomicAdd(&s_ncand, 1u);
-                cand[pos] = ((unsigned long long)float_order_key(cur) << 32) | (uint32_t)(~i);
+            unsigned long long v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = linefit_rxyw((uint32_t)k[u], F.width, F.height, F.grey);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t i = i0 + u * blockDim.x;
+                if (i < n) {
+                    const uint32_t packed = (uint32_t)k[u];
+                    atag_cluster_point cp;
+                    cp.packed_x = (uint16_t)packed;
+                    cp.packed_y = (uint16_t)(packed >> 16);
+                    cp.slope = float_from_order_key((uint32_t)(k[u] >> 32));
+                    F.cluster_points[start + i] = cp;
+                    X[i] = v[u];
+                }
             }
         }
         __syncthreads();
-        const uint32_t npeaks = s_ncand;
-        // the 10 best by (error desc, index asc): repeated block argmax
+        // segmented inclusive scan of the moments (main.cpp:796-801): warp w
+        // owns a contiguous range of 32-point chunks; warp totals first, then
+        // chunk by chunk a warp scan plus the running carry, so consecutive
+        // lanes store consecutive LineFitPoints
+        {
+            constexpr uint32_t W = THREADS / 32;
+            const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+            const uint32_t nch = (n + 31) / 32, ch0 = nch * w / W, ch1 = nch * (w + 1) / W;
+            Moment t{0, 0, 0, 0, 0, 0};
+            for (uint32_t c = ch0; c < ch1; c++) {
+                const uint32_t i = c * 32 + lane;
+                if (i < n) t = m_add(t, moment_of(X[i]));
+            }
+            t = warp_sum_moment(t);
+            if (lane == 0) {
+                red_m[w][0] = t.Mx; red_m[w][1] = t.My; red_m[w][2] = t.Mxx;
+                red_m[w][3] = t.Myy; red_m[w][4] = t.Mxy; red_m[w][5] = t.W;
+            }
+            __syncthreads();
+            Moment carry{0, 0, 0, 0, 0, 0};
+            for (uint32_t k = 0; k < w; k++)
+                carry = m_add(carry, Moment{red_m[k][0], red_m[k][1], red_m[k][2], red_m[k][3], red_m[k][4],
+                                            red_m[k][5]});
+            for (uint32_t c = ch0; c < ch1; c++) {
+                const uint32_t i = c * 32 + lane;
+                const Moment v = i < n ? moment_of(X[i]) : Moment{0, 0, 0, 0, 0, 0};
+                const Moment incl = warp_inclusive_scan_moment(v);
+                if (i < n) store_moment(F.line_fit + start + i, m_add(carry, incl));
+                carry = m_add(carry, shfl_moment(incl, 31));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(CF_SMALL_THREADS) k_cluster_sort_small(const __grid_constant__ FrameSet fs,
+                                                                        const uint32_t* __restrict__ work_offsets,
+                                                                        uint32_t n_frames,
+                                                                        uint32_t* __restrict__ work_counter,
+                                                                        uint32_t sort_cap) {
+    cluster_sort<false>(fs, work_offsets, n_frames, work_counter, sort_cap);
+}
+__global__ void __launch_bounds__(CF_LARGE_THREADS, 1) k_cluster_sort_large(const __grid_constant__ FrameSet fs,
+                                                                           const uint32_t* __restrict__ work_offsets,
+                                                                           uint32_t n_frames,
+                                                                           uint32_t* __restrict__ work_counter) {
+    cluster_sort<true>(fs, work_offsets, n_frames, work_counter, CF_LARGE_CAP);
+}
+
+// ---------------------------------------------------------------------------
+// 4b. fit_lines (fit_quad.cpp:153-375) in its cyclic form: the error of the
+// window around each point, the 7-tap filter and the strict local maxima.
+// One warp per run of up to CE_RUN consecutive points of one cluster, 32
+// points per step: the warp keeps the errors of positions [s-4, s+36) and
+// the filtered errors of [s-1, s+33) in shared memory (cluster-local,
+// cyclic indices), carrying the last 8 errors into the next step.  Maxima
+// are appended to their cluster's candidate list, which reuses the
+// cluster's segment of the sort-key buffer (a cyclic sequence of n values
+// has at most n/2 strict maxima).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t cyclic(int i, int n) {  // i in [-n, 3n)
+    if (i < 0) i += n;
+    while (i >= n) i -= n;
+    return (uint32_t)i;
+}
+
+constexpr int CE_WARPS = 8;
+
+__global__ void __launch_bounds__(32 * CE_WARPS) k_cluster_errors(const __grid_constant__ FrameSet fs,
+                                                                  const uint32_t* __restrict__ run_offsets,
+                                                                  uint32_t n_frames,
+                                                                  uint32_t* __restrict__ work_counter) {
+    __shared__ float s_err[CE_WARPS][40];
+    __shared__ float s_flt[CE_WARPS][34];
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float* e = s_err[wid];
+    float* f = s_flt[wid];
+    const uint32_t total = run_offsets[n_frames];
+    for (;;) {
+        uint32_t item = 0;
+        if (lane == 0) item = atomicAdd(work_counter, 1u);
+        item = __shfl_sync(0xffffffffu, item, 0);
+        if (item >= total) return;
+        const uint32_t fidx = find_frame(run_offsets, n_frames, item);
+        const FrameDesc& F = fs.get(fidx);
+        const uint32_t r = item - run_offsets[fidx];
+        // the cluster whose runs contain r
+        uint32_t lo = 0, hi = F.counters[CNT_CLUSTERS];
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (F.cluster_runs[mid] <= r) lo = mid; else hi = mid;
+        }
+        const uint32_t cid = lo;
+        const atag_cluster_extents ext = F.cluster_extents[cid];
+        const int n = (int)ext.count;
+        const uint32_t k = min(20u, ext.count / 12u);
+        const atag_line_fit_point* pts = F.line_fit + ext.start;
+        const int li0 = (int)((r - F.cluster_runs[cid]) * CE_RUN);
+        const int li1 = min(n, li0 + (int)CE_RUN);
+        for (int s = li0; s < li1; s += 32) {
+            if (s == li0) {
+                e[lane] = window_error_local(pts, n, k, cyclic(s - 4 + (int)lane, n));
+                if (lane < 8) e[32 + lane] = window_error_local(pts, n, k, cyclic(s + 28 + (int)lane, n));
+            } else {
+                const float carry = lane < 8 ? e[32 + lane] : 0.0f;
+                __syncwarp();
+                if (lane < 8) e[lane] = carry;
+                e[8 + lane] = window_error_local(pts, n, k, cyclic(s + 4 + (int)lane, n));
+            }
+            __syncwarp();
+            // cyclic 7-tap filter (fit_quad.cpp:296-324): f[j] is position s - 1 + j
+            {
+                float acc = 0.0f;
+#pragma unroll
+                for (int j = 0; j < 7; j++) acc = __fadd_rn(acc, __fmul_rn(e[lane + j], filter_tap(j)));
+                f[lane] = acc;
+                if (lane < 2) {
+                    float a2 = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < 7; j++) a2 = __fadd_rn(a2, __fmul_rn(e[32 + lane + j], filter_tap(j)));
+                    f[32 + lane] = a2;
+                }
+            }
+            __syncwarp();
+            // strict local maxima (fit_quad.cpp:341-371) with error != 0
+            // (main.cpp:832-835); global point 0 is never a corner (the
+            // first work-group's first output is x = 1, fit_quad.cpp:182-190)
+            const int li = s + (int)lane;
+            if (li < li1) {
+                const float cur = f[lane + 1];
+                if (cur > f[lane] && cur > f[lane + 2] && cur != 0.0f && !(cid == 0 && li == 0)) {
+                    const uint32_t at = atomicAdd(F.peak_count + cid, 1u);
+                    F.sortbuf[ext.start + at] =
+                        ((unsigned long long)float_order_key(cur) << 32) | (uint32_t)(~(uint32_t)li);
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4c. the 10 best peaks of each cluster by (error desc, index asc): the
+// corner sort of main.cpp:856-863 restricted to what do_indexing reads
+// (fit_quad.cpp:411-414 uses at most 10 corners).  One warp per cluster.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_cluster_peaks(const __grid_constant__ FrameSet fs,
+                                                       const uint32_t* __restrict__ cluster_offsets,
+                                                       uint32_t n_frames) {
+    const uint32_t lane = threadIdx.x & 31, wpb = blockDim.x >> 5;
+    const uint32_t total = cluster_offsets[n_frames];
+    for (uint32_t item = blockIdx.x * wpb + (threadIdx.x >> 5); item < total; item += gridDim.x * wpb) {
+        const uint32_t fidx = find_frame(cluster_offsets, n_frames, item);
+        const FrameDesc& F = fs.get(fidx);
+        const uint32_t cid = item - cluster_offsets[fidx];
+        const uint32_t npeaks = F.peak_count[cid];
+        const unsigned long long* cand = F.sortbuf + F.cluster_extents[cid].start;
+        const uint32_t take = npeaks < 10u ? npeaks : 10u;
         unsigned long long last = ~0ull;
-        const uint32_t take = npeaks < 10 ? npeaks : 10;
         for (uint32_t j = 0; j < take; j++) {
             unsigned long long best = 0;
-            for (uint32_t c = threadIdx.x; c < npeaks; c += blockDim.x) {
-                unsigned long long key = cand[c];
+            for (uint32_t c = lane; c < npeaks; c += 32) {
+                const unsigned long long key = cand[c];
                 if (key < last && key > best) best = key;
             }
-            best = block_max_u64(best, red64);
-            if (threadIdx.x == 0) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long v = __shfl_xor_sync(0xffffffffu, best, o);
+                best = v > best ? v : best;
+            }
+            if (lane == 0) {
                 atag_corner c;
                 c.line_fit_point_index = ~(uint32_t)best;
                 c.cluster_index = (uint16_t)cid;
@@ -635,21 +824,7 @@ __device__ __forceinline__ void cluster_fit(const FrameSet& fs, const uint32_t* 
             }
             last = best;
         }
-        if (threadIdx.x == 0) F.peak_count[cid] = npeaks;
     }
-}
-
-__global__ void __launch_bounds__(CF_SMALL_THREADS, 4) k_cluster_fit_small(const __grid_constant__ FrameSet fs,
-                                                                          const uint32_t* __restrict__ work_offsets,
-                                                                          uint32_t n_frames,
-                                                                          uint32_t* __restrict__ work_counter) {
-    cluster_fit<false>(fs, work_offsets, n_frames, work_counter);
-}
-__global__ void __launch_bounds__(CF_LARGE_THREADS, 1) k_cluster_fit_large(const __grid_constant__ FrameSet fs,
-                                                                          const uint32_t* __restrict__ work_offsets,
-                                                                          uint32_t n_frames,
-                                                                          uint32_t* __restrict__ work_counter) {
-    cluster_fit<true>(fs, work_offsets, n_frames, work_counter);
 }
 
 // ---------------------------------------------------------------------------

@@ -211,10 +211,21 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __shared__ uint32_t par[2 * CCL_THREADS];
     __shared__ uint32_t cnt[2 * CCL_THREADS];
 
-    for (int i = threadIdx.x; i < PH * PW; i += blockDim.x) {
-        int r = i / PW, c = i % PW;
-        int y = y0 - 1 + r, x = x0 - 1 + c;
-        pix[r][c] = (x >= 0 && x < w && y >= 0 && y < h) ? F.thr[(size_t)y * w + x] : 127;
+    // the tile's pixels plus a one-pixel halo (x0 - 1 .. x0 + 2 CCL_BX, y0 - 1
+    // ..), loaded as aligned 32-bit words (x0 and w are multiples of 4)
+    {
+        constexpr int WPR = (2 * CCL_BX + 8) / 4;  // words x0 - 4 .. x0 + 2 CCL_BX + 3
+        const uint32_t* thr32 = reinterpret_cast<const uint32_t*>(F.thr);
+        for (int i = threadIdx.x; i < PH * WPR; i += blockDim.x) {
+            const int r = i / WPR, k = i % WPR;
+            const int y = y0 - 1 + r, xw = x0 - 4 + 4 * k;
+            const uint32_t v = (y >= 0 && y < h && xw >= 0 && xw < w) ? thr32[((size_t)y * w + xw) / 4] : 0x7F7F7F7Fu;
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const int c = xw + b - (x0 - 1);
+                if (c >= 0 && c < PW) pix[r][c] = (uint8_t)(v >> (8 * b));
+            }
+        }
     }
     const int tx = threadIdx.x % CCL_BX, ty = threadIdx.x / CCL_BX;
     const int bx = bx0 + tx, by = by0 + ty;
@@ -266,7 +277,10 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
 }
 
 // Merge the links that cross tile borders: P/Q/R of the tile's top row,
-// P/S of its left column and R (up-right) of its right column.
+// P/S of its left column and R (up-right) of its right column.  After the
+// local pass every slot points at its tile root, so a link is a union of
+// two tile roots; a lane skips a union that the lane before it (the
+// previous block of the same tile edge) makes too.
 template <int CCL_BY>
 __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
     constexpr int CCL_BORDER_PER_TILE = CCL_BX + 2 * (CCL_BY - 1);
@@ -276,64 +290,115 @@ __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
     const int per_tile = CCL_BORDER_PER_TILE;
     const int total = ntx * nty * per_tile;
     volatile uint32_t* par = F.scratch;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        int tile = i / per_tile, k = i % per_tile;
-        int tbx = (tile % ntx) * CCL_BX, tby = (tile / ntx) * CCL_BY;
-        int bx, by;
-        if (k < CCL_BX) { bx = tbx + k; by = tby; }
-        else if (k < CCL_BX + CCL_BY - 1) { bx = tbx; by = tby + 1 + (k - CCL_BX); }
-        else { bx = tbx + CCL_BX - 1; by = tby + 1 + (k - CCL_BX - (CCL_BY - 1)); }
-        if (bx >= w / 2 || by >= h / 2) continue;
+    const int lane = threadIdx.x & 31;
+    bool ok = true;
+    // warp-uniform trip count: lanes past the end take part in the votes
+    for (int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < total; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + lane;
+        int tbx = 0, tby = 0, bx = 0, by = 0;
+        bool live = i < total;
+        if (live) {
+            const int tile = i / per_tile, k = i % per_tile;
+            tbx = (tile % ntx) * CCL_BX;
+            tby = (tile / ntx) * CCL_BY;
+            if (k < CCL_BX) { bx = tbx + k; by = tby; }
+            else if (k < CCL_BX + CCL_BY - 1) { bx = tbx; by = tby + 1 + (k - CCL_BX); }
+            else { bx = tbx + CCL_BX - 1; by = tby + 1 + (k - CCL_BX - (CCL_BY - 1)); }
+            live = bx < w / 2 && by < h / 2;
+        }
+        BlockLinks L{0, 0, 0};
         const int x = bx * 2, y = by * 2;
-        const uint8_t* base = F.thr + (size_t)y * w + x;
-        BlockLinks L = block_links([&](int dy, int dx) { return (uint32_t)base[(ptrdiff_t)dy * w + dx]; }, x, y, w, h);
+        if (live) {
+            const uint8_t* base = F.thr + (size_t)y * w + x;
+            L = block_links([&](int dy, int dx) { return (uint32_t)base[(ptrdiff_t)dy * w + dx]; }, x, y, w, h);
+        }
         const int ndx[4] = {-1, 0, 1, -1}, ndy[4] = {-1, -1, -1, 0};
         const uint32_t sid = (uint32_t)y * w + x;
-        bool ok = true;
 #pragma unroll
         for (int n = 0; n < 4; n++) {
-            int nbx = bx + ndx[n], nby = by + ndy[n];
-            // same tile?  then it was merged locally
-            if (nbx >= tbx && nbx < tbx + CCL_BX && nby >= tby) continue;
-            uint32_t nid = (uint32_t)(nby * 2) * w + nbx * 2;
-            if (L.wmask & (1u << n)) ok &= uf_union(par, sid, nid);
-            if (L.bmask & (1u << n)) ok &= uf_union(par, sid + 1, nid + 1);
+            const int nbx = bx + ndx[n], nby = by + ndy[n];
+            // a neighbour in the same tile was merged by the local pass
+            const bool cross = live && !(nbx >= tbx && nbx < tbx + CCL_BX && nby >= tby);
+            const uint32_t nid = (uint32_t)(nby * 2) * w + nbx * 2;
+            const bool lw = cross && (L.wmask & (1u << n)), lb = cross && (L.bmask & (1u << n));
+            const uint32_t aw = lw ? par[sid] : 0u, bw = lw ? par[nid] : 0u;
+            const uint32_t ab = lb ? par[sid + 1] : 0u, bb = lb ? par[nid + 1] : 0u;
+            const unsigned long long kw = lw ? ((unsigned long long)aw << 32 | bw) : ~0ull;
+            const unsigned long long kb = lb ? ((unsigned long long)ab << 32 | bb) : ~0ull;
+            const unsigned long long pw = __shfl_up_sync(0xFFFFFFFFu, kw, 1), pb = __shfl_up_sync(0xFFFFFFFFu, kb, 1);
+            if (lw && (lane == 0 || pw != kw)) ok &= uf_union(par, aw, bw);
+            if (lb && (lane == 0 || pb != kb)) ok &= uf_union(par, ab, bb);
         }
-        if (!ok && F.counters) atomicOr(F.counters + CNT_STATUS, ATAG_DEVFLAG_UF_ITERATION_CAP);
     }
+    if (!ok && F.counters) atomicOr(F.counters + CNT_STATUS, ATAG_DEVFLAG_UF_ITERATION_CAP);
 }
 
 // FINAL_LABELLING (segmentation.cpp:316-389): labels, component sizes at
-// the root, parent array compressed to roots.
+// the root, parent array compressed to roots.  A thread takes two
+// horizontally adjacent 2x2 blocks (four slots: 16-byte loads and stores of
+// parents, sizes and labels) and follows the four parent chains in lock
+// step, so four dependent loads are in flight at once.  The forest is final
+// here; the only concurrent writes replace a parent by its root, so any
+// value read is an ancestor.
 __global__ void __launch_bounds__(256) k_ccl_final(const __grid_constant__ FrameSet fs) {
     const FrameDesc& F = fs.get(blockIdx.y);
     const int w = F.width, h = F.height;
-    const int nbx = w / 2, nb = nbx * (h / 2);
-    volatile uint32_t* par = F.scratch;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += gridDim.x * blockDim.x) {
-        const int bx = i % nbx, by = i / nbx;
-        const size_t id = (size_t)(by * 2) * w + bx * 2;
-        const uint32_t sw = (uint32_t)id, sb = (uint32_t)id + 1;
-        const uint32_t rw = find_root_volatile(par, sw), rb = find_root_volatile(par, sb);
-        // compress: every slot ends pointing at its root, as the reference's
-        // scratch does after its last compression (segmentation.cpp:309)
-        par[sw] = rw;
-        par[sb] = rb;
-        const uint32_t cw = F.sizes[sw], cb = F.sizes[sb];
-        if (rw != sw) {
-            if (cw) atomicAdd(F.sizes + rw, cw);
-            F.sizes[sw] = 0;
+    const int npx = w / 4, np = npx * (h / 2);  // block pairs (w % 4 == 0)
+    const uint32_t* par = F.scratch;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        const int px = i % npx, by = i / npx;
+        const size_t id = (size_t)(by * 2) * w + (size_t)px * 4;
+        const uint4 p4 = *reinterpret_cast<const uint4*>(F.scratch + id);
+        const uint4 s4 = *reinterpret_cast<const uint4*>(F.sizes + id);
+        const uint32_t top = *reinterpret_cast<const uint32_t*>(F.thr + id);
+        const uint32_t bot = *reinterpret_cast<const uint32_t*>(F.thr + id + w);
+        uint32_t r[4] = {p4.x, p4.y, p4.z, p4.w};
+        bool capped = true;
+        for (uint32_t it = 0; it < UF_FIND_CAP; it++) {
+            uint32_t q[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) q[k] = par[r[k]];
+            bool done = true;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                done &= q[k] == r[k];
+                r[k] = q[k];
+            }
+            if (done) {
+                capped = false;
+                break;
+            }
         }
-        if (rb != sb) {
-            if (cb) atomicAdd(F.sizes + rb, cb);
-            F.sizes[sb] = 0;
+        if (capped && F.counters) atomicOr(F.counters + CNT_STATUS, ATAG_DEVFLAG_UF_ITERATION_CAP);
+        // every slot ends pointing at its root, as the reference's scratch
+        // does after its last compression (segmentation.cpp:309)
+        *reinterpret_cast<uint4*>(F.scratch + id) = make_uint4(r[0], r[1], r[2], r[3]);
+        // fold the tile counts of non-root slots into their roots; a root's
+        // own entry is left alone (other threads add to it)
+        const uint32_t sz[4] = {s4.x, s4.y, s4.z, s4.w};
+        bool any_root = false;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint32_t sid = (uint32_t)id + k;
+            if (r[k] == sid) any_root = true;
+            else if (sz[k]) atomicAdd(F.sizes + r[k], sz[k]);
         }
-        const uint8_t* t = F.thr + id;
-        const uchar2 top = *reinterpret_cast<const uchar2*>(t);
-        const uchar2 bot = *reinterpret_cast<const uchar2*>(t + w);
-        auto lab = [&](uint8_t c) { return c == 255 ? (LABEL_PIXEL_MASK | rw) : (c == 0 ? rb : 0u); };
-        *reinterpret_cast<uint2*>(F.labels + id) = make_uint2(lab(top.x), lab(top.y));
-        *reinterpret_cast<uint2*>(F.labels + id + w) = make_uint2(lab(bot.x), lab(bot.y));
+        if (!any_root) {
+            *reinterpret_cast<uint4*>(F.sizes + id) = make_uint4(0u, 0u, 0u, 0u);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (r[k] != (uint32_t)id + k) F.sizes[id + k] = 0u;
+        }
+        auto lab = [](uint32_t c, uint32_t rw, uint32_t rb) {
+            return c == 255u ? (LABEL_PIXEL_MASK | rw) : (c == 0u ? rb : 0u);
+        };
+        *reinterpret_cast<uint4*>(F.labels + id) =
+            make_uint4(lab(top & 255u, r[0], r[1]), lab((top >> 8) & 255u, r[0], r[1]),
+                       lab((top >> 16) & 255u, r[2], r[3]), lab(top >> 24, r[2], r[3]));
+        *reinterpret_cast<uint4*>(F.labels + id + w) =
+            make_uint4(lab(bot & 255u, r[0], r[1]), lab((bot >> 8) & 255u, r[0], r[1]),
+                       lab((bot >> 16) & 255u, r[2], r[3]), lab(bot >> 24, r[2], r[3]));
     }
 }
 

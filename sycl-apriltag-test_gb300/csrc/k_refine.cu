@@ -77,7 +77,8 @@ struct LaneState {
     Bilinear s[2];
     float sx[2], sy[2];
     // position-level values (valid on even lanes)
-    float v[4], gd[3], w[3], Om, Nn, o, qx, qy, W;
+    float v[4], gd[3], w[3], Om, Nn, o, W;
+    float sa;              // (t_j - 1/2) |b - a|: q_j - midpoint = sa d + o n
     float nux, nuy, dist;  // normal of the fitted line, distance of q_j to it
 };
 
@@ -116,12 +117,13 @@ __device__ __forceinline__ void edge_forward(const float* __restrict__ img, int 
         L.Nn += L.w[m] * (float)(m - 1);
     }
     L.o = L.Nn / (L.Om + RF_EPS);
-    L.qx = px + L.o * L.nx;
-    L.qy = py + L.o * L.ny;
     L.W = L.Om + RF_EPS;  // a contrast-free edge falls back to the unrefined line
-    // moments about the edge midpoint, one contribution per position
+    // moments about the edge midpoint, one contribution per position; the
+    // point is taken relative to the midpoint in the edge's own frame
+    // ((j - 7.5) / 16 is exact), not as a difference of image coordinates
     const float ox = 0.5f * (ax + bx), oy = 0.5f * (ay + by);
-    const float X = L.qx - ox, Y = L.qy - oy, Wc = half ? 0.0f : L.W;
+    L.sa = ((float)j - 0.5f * (RF_POS - 1)) / (float)RF_POS * L.len;
+    const float X = L.sa * L.dx + L.o * L.nx, Y = L.sa * L.dy + L.o * L.ny, Wc = half ? 0.0f : L.W;
     float m6[6] = {Wc, Wc * X, Wc * Y, Wc * X * X, Wc * Y * Y, Wc * X * Y};
 #pragma unroll
     for (int k = 0; k < 6; k++)
@@ -144,10 +146,16 @@ __device__ __forceinline__ void edge_forward(const float* __restrict__ img, int 
     E.ux = cos(E.phi);
     E.uy = sin(E.phi);
     // residual sum W_j d_j^2 of the perpendicular distances to the fitted
-    // line, in a second pass (S0 * lambda_min from the moments would cancel)
-    L.nux = (float)(-E.uy);
-    L.nuy = (float)E.ux;
-    L.dist = (X - (float)mx) * L.nux + (Y - (float)my) * L.nuy;
+    // line, in a second pass (S0 * lambda_min from the moments would
+    // cancel), in the edge frame: d_j = sa (d.nu) + o (n.nu) - (m.nu), whose
+    // terms are small where the line runs along the edge
+    const double nux = -E.uy, nuy = E.ux;
+    L.nux = (float)nux;
+    L.nuy = (float)nuy;
+    const float cs = (float)((double)L.dx * nux + (double)L.dy * nuy);
+    const float cn = (float)((double)L.nx * nux + (double)L.ny * nuy);
+    const float c0 = (float)(mx * nux + my * nuy);
+    L.dist = L.sa * cs + L.o * cn - c0;
     float rr = half ? 0.0f : L.W * L.dist * L.dist;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) rr += __shfl_xor_sync(0xffffffffu, rr, off);
@@ -276,16 +284,15 @@ __global__ void __launch_bounds__(128) k_refine_backward(const float* __restrict
     const double gSx = gmx / E.S0, gSy = gmy / E.S0;
     gS0 += -(E.Sxx * gcxx + E.Syy * gcyy + E.Sxy * gcxy + E.Sx * gmx + E.Sy * gmy) / (E.S0 * E.S0);
     // moments -> edge point q_j and weight W_j (even lanes own position j)
-    const float ox = 0.5f * (L.ax + L.bx), oy = 0.5f * (L.ay + L.by);
-    const float X = L.qx - ox, Y = L.qy - oy;
+    const float X = L.sa * L.dx + L.o * L.nx, Y = L.sa * L.dy + L.o * L.ny;
     const float grf = (float)gr;
     float gW = (float)(gS0 + gSx * X + gSy * Y + gSxx * X * X + gSyy * Y * Y + gSxy * X * Y) +
                grf * L.dist * L.dist;
     float gqx = (float)(L.W * (gSx + 2.0 * gSxx * X + gSxy * Y)) + grf * 2.0f * L.W * L.dist * L.nux;
     float gqy = (float)(L.W * (gSy + 2.0 * gSyy * Y + gSxy * X)) + grf * 2.0f * L.W * L.dist * L.nuy;
-    // the moments were taken about the midpoint (ox, oy): X = qx - ox
+    // X = q_x - o_x with q = p + o n and o the midpoint (the forward
+    // evaluates the same quantity as sa d_x + o n_x)
     float gox = -gqx, goy = -gqy;
-    // q = p + o n
     float gpx = gqx, gpy = gqy;
     const float go = gqx * L.nx + gqy * L.ny;
     float gnx = L.o * gqx, gny = L.o * gqy;
