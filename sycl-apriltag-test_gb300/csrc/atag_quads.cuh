@@ -78,95 +78,104 @@ __device__ __forceinline__ uint32_t block_min_u32(uint32_t v, uint32_t* red) {
     return red[0];
 }
 
-// The group minimum and "lowest combination within 0.1 of it"
-// (fit_quad.cpp:501-519).  Returns the chosen combination number or -1.
-__device__ __forceinline__ int choose_combination(float err, uint32_t n, unsigned long long* red64,
-                                                  uint32_t* red32) {
-    (void)red64;
-    uint32_t key = float_order_key(err);
-    uint32_t lowest_key = block_min_u32(key, red32);
-    float lowest = float_from_order_key(lowest_key);
-    if (isinf(lowest) && lowest > 0) return -1;
-    bool q = __fsub_rn(err, lowest) < 0x1.99999ap-4f;  // (double)(err - lowest) < 0.1, in float
-    uint32_t chosen = block_min_u32(q ? n : 0xFFFFFFFFu, red32);
-    return chosen == 0xFFFFFFFFu ? -1 : (int)chosen;
-}
-
-// do_indexing for one peak cluster on a 256-thread CTA.  The 210
-// combinations of up to 10 peaks only ever fit the 90 ordered segments
-// between two of those peaks, so each segment is fitted once (the same
-// get_moment/fit_line calls as the per-combination form, hence the same
-// bits) and every combination sums four table entries in the reference's
-// order (fit_quad.cpp:445-498).  Writes *out only when a combination is
-// chosen; returns the chosen number or -1.
+// do_indexing for one peak cluster on one warp.  The 210 combinations of
+// up to 10 peaks only ever fit the 90 ordered segments between two of those
+// peaks, so each segment is fitted once (the same get_moment/fit_line calls
+// as the per-combination form, hence the same bits) and every combination
+// sums four table entries in the reference's order (fit_quad.cpp:445-498).
+// The choice is the reference's: the lowest total error, then the smallest
+// combination number within 0.1 of it (fit_quad.cpp:501-519).  The lane
+// that owns the chosen combination writes *out (its moments recomputed by
+// the same calls); every lane returns the chosen number, or -1.
 struct SegmentTable {
     float err[10][10], mse[10][10], lp[10][10][4];
-    Moment m[10][10];
-    uint16_t nim[10][10];
     uint32_t idx[10];        // line_fit_point_index of peak rank r
 };
 
 __device__ __forceinline__ int index_one_cluster(uint32_t count, const atag_corner* __restrict__ corners,
                                                  const atag_line_fit_point* __restrict__ cpts, uint32_t ccount,
                                                  float max_mse, float cos_critical, SegmentTable& T,
-                                                 uint32_t* red32, atag_fitted_quad* out) {
+                                                 atag_fitted_quad* out) {
+    constexpr int PER = (210 + 31) / 32;  // combinations per lane
+    const uint32_t lane = threadIdx.x & 31;
     const uint32_t m = count < 10u ? count : 10u;
     const uint32_t ncomb = n_choose_4(m);
     if (ncomb == 0) return -1;
-    if (threadIdx.x < m) T.idx[threadIdx.x] = corners[threadIdx.x].line_fit_point_index;
-    __syncthreads();
-    for (uint32_t s = threadIdx.x; s < m * m; s += blockDim.x) {
+    if (lane < m) T.idx[lane] = corners[lane].line_fit_point_index;
+    __syncwarp();
+    for (uint32_t s = lane; s < m * m; s += 32) {
         const uint32_t a = s / m, b = s % m;
         if (a == b) continue;
         const unsigned long long i0 = T.idx[a], i1 = T.idx[b];
         unsigned long long nim;
-        Moment mo = get_moment(cpts, ccount, i0, i1, &nim);
+        const Moment mo = get_moment(cpts, ccount, i0, i1, &nim);
         float e, mse;
         fit_line(mo, nim, i0 < i1 ? T.lp[a][b] : nullptr, &e, &mse);
         T.err[a][b] = e;
         T.mse[a][b] = mse;
-        T.m[a][b] = mo;
-        T.nim[a][b] = (uint16_t)nim;
     }
-    __syncthreads();
-    const uint32_t n = threadIdx.x;
-    float err = __int_as_float(0x7f800000);
-    uint32_t r[4] = {0, 0, 0, 0};
-    if (n < ncomb) {
+    __syncwarp();
+    // the ranks of combination n in line-fit index order (sort_4,
+    // fit_quad.cpp:437)
+    auto ranks = [&](uint32_t n, uint32_t (&r)[4]) {
         uint32_t d[4];
         combination_decode(n, d);
-        // sort_4 on the line-fit indices (fit_quad.cpp:437), tracking ranks
         unsigned long long v[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) v[j] = ((unsigned long long)T.idx[d[j]] << 8) | d[j];
         sort_4(v);
 #pragma unroll
         for (int j = 0; j < 4; j++) r[j] = (uint32_t)(v[j] & 0xFF);
-        float total = 0.0f;
-        bool valid = true;
+    };
+    float errs[PER];
+    uint32_t low_key = float_order_key(__int_as_float(0x7f800000));
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const uint32_t a = r[j], b = r[(j + 1) & 3];
-            valid &= T.mse[a][b] <= max_mse;
-            total = __fadd_rn(total, T.err[a][b]);
+    for (int t = 0; t < PER; t++) {
+        const uint32_t n = lane + 32u * t;
+        float err = __int_as_float(0x7f800000);
+        if (n < ncomb) {
+            uint32_t r[4];
+            ranks(n, r);
+            float total = 0.0f;
+            bool valid = true;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const uint32_t a = r[j], b = r[(j + 1) & 3];
+                valid &= T.mse[a][b] <= max_mse;
+                total = __fadd_rn(total, T.err[a][b]);
+            }
+            const float* p01 = T.lp[r[0]][r[1]];
+            const float* p12 = T.lp[r[1]][r[2]];
+            const float dot = __fadd_rn(__fmul_rn(p01[2], p12[2]), __fmul_rn(p01[3], p12[3]));
+            valid &= fabsf(dot) <= cos_critical;
+            if (valid && !isnan(total)) err = total;
         }
-        const float* p01 = T.lp[r[0]][r[1]];
-        const float* p12 = T.lp[r[1]][r[2]];
-        float dot = __fadd_rn(__fmul_rn(p01[2], p12[2]), __fmul_rn(p01[3], p12[3]));
-        valid &= fabsf(dot) <= cos_critical;
-        if (valid && !isnan(total)) err = total;
+        errs[t] = err;
+        low_key = min(low_key, float_order_key(err));
     }
-    const int chosen = choose_combination(err, n, nullptr, red32);
-    if (chosen >= 0 && (int)n == chosen) {
+    low_key = __reduce_min_sync(0xFFFFFFFFu, low_key);
+    const float lowest = float_from_order_key(low_key);
+    if (isinf(lowest) && lowest > 0) return -1;
+    uint32_t first = 0xFFFFFFFFu;
+#pragma unroll
+    for (int t = PER - 1; t >= 0; t--)  // (double)(err - lowest) < 0.1, in float
+        if (__fsub_rn(errs[t], lowest) < 0x1.99999ap-4f) first = lane + 32u * t;
+    const uint32_t chosen = __reduce_min_sync(0xFFFFFFFFu, first);
+    if (chosen == 0xFFFFFFFFu) return -1;
+    if (lane == (chosen & 31u)) {
+        uint32_t r[4];
+        ranks(chosen, r);
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             const uint32_t a = r[j], b = r[(j + 1) & 3];
-            store_moment(&out->moments[j], T.m[a][b]);
-            out->num_in_moments[j] = T.nim[a][b];
+            unsigned long long nim;
+            const Moment mo = get_moment(cpts, ccount, T.idx[a], T.idx[b], &nim);
+            store_moment(&out->moments[j], mo);
+            out->num_in_moments[j] = (uint16_t)nim;
             out->indices[j] = (uint16_t)T.idx[a];
         }
     }
-    return chosen;
+    return (int)chosen;
 }
 
 __device__ __forceinline__ void write_fitted(atag_fitted_quad* out, const Combination& c) {

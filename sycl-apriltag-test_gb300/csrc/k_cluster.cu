@@ -858,10 +858,10 @@ __global__ void __launch_bounds__(1024) k_peaks_scan(const __grid_constant__ Fra
 __global__ void __launch_bounds__(256) k_index_quads(const __grid_constant__ FrameSet fs,
                                                      const uint32_t* __restrict__ work_offsets, uint32_t n_frames,
                                                      PipelineParams p) {
-    __shared__ SegmentTable T;
-    __shared__ uint32_t red32[33];
+    __shared__ SegmentTable T[8];  // one per warp
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t total = work_offsets[n_frames];
-    for (uint32_t item = blockIdx.x; item < total; item += gridDim.x) {
+    for (uint32_t item = blockIdx.x * 8 + wid; item < total; item += gridDim.x * 8) {
         const uint32_t fidx = find_frame(work_offsets, n_frames, item);
         const FrameDesc& F = fs.get(fidx);
         const uint32_t q = item - work_offsets[fidx];
@@ -869,18 +869,18 @@ __global__ void __launch_bounds__(256) k_index_quads(const __grid_constant__ Fra
         const atag_cluster_extents ce = F.cluster_extents[p.compat_peak_index ? q : cid];
         atag_fitted_quad* fq = F.fitted + q;
         const int chosen = index_one_cluster(F.peak_count[cid], F.peaks + (size_t)cid * 10, F.line_fit + ce.start,
-                                             ce.count, p.max_line_fit_mse, p.cos_critical_f, T, red32, fq);
+                                             ce.count, p.max_line_fit_mse, p.cos_critical_f, T[wid], fq);
         if (chosen < 0) {
             // no combination: the quad stays zero (main.cpp:318-319)
-            if (threadIdx.x < sizeof(atag_fitted_quad) / 4) reinterpret_cast<uint32_t*>(fq)[threadIdx.x] = 0u;
-            if (threadIdx.x == 0) F.quad_ok[q] = 0;
-        } else if ((int)threadIdx.x == chosen) {
+            for (uint32_t k = lane; k < sizeof(atag_fitted_quad) / 4; k += 32) reinterpret_cast<uint32_t*>(fq)[k] = 0u;
+            if (lane == 0) F.quad_ok[q] = 0;
+        } else if (lane == ((uint32_t)chosen & 31u)) {
             atag_quad_corners qc;
-            bool ok = quad_corners(*fq, p, q, &qc);
+            const bool ok = quad_corners(*fq, p, q, &qc);
             F.quad_tmp[q] = qc;
             F.quad_ok[q] = ok ? 1u : 0u;
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 

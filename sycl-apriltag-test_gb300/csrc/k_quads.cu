@@ -83,14 +83,14 @@ __global__ void __launch_bounds__(256) k_do_indexing(const atag_peak_extents* __
                                                      const atag_cluster_extents* __restrict__ cluster_extents,
                                                      float max_mse, float cos_critical,
                                                      atag_fitted_quad* __restrict__ fitted) {
-    __shared__ SegmentTable T;
-    __shared__ uint32_t redu[33];
-    for (size_t q = blockIdx.x; q < count; q += gridDim.x) {
+    __shared__ SegmentTable T[8];  // one per warp
+    const uint32_t wid = threadIdx.x >> 5;
+    for (size_t q = (size_t)blockIdx.x * 8 + wid; q < count; q += (size_t)gridDim.x * 8) {
         const atag_peak_extents pe = extents[q];
         const atag_cluster_extents ce = cluster_extents[q];
-        index_one_cluster(pe.count, corners + pe.start, points + ce.start, ce.count, max_mse, cos_critical, T, redu,
+        index_one_cluster(pe.count, corners + pe.start, points + ce.start, ce.count, max_mse, cos_critical, T[wid],
                           fitted + q);
-        __syncthreads();
+        __syncwarp();
     }
 }
 
