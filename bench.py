@@ -119,24 +119,26 @@ class ClockSampler:
 
 
 def stage_bytes(stats, n_src_px):
-    """Algorithmic bytes per stage for the whole batch (minimum logical
-    traffic of each kernel's contract; one read or write per array)."""
+    """Algorithmic bytes per stage for the whole batch: the minimum logical
+    traffic of each kernel's contract (every array element it must read or
+    write, once; gathers that hit the same element again are not counted).
+    N pixels, Pf points of surviving clusters, C pairs, Cp clusters with
+    peaks (the FrameStats counts)."""
     N = sum(int(s["width"]) * int(s["height"]) for s in stats)
-    P = sum(int(s["n_points"]) for s in stats)
     C = sum(int(s["n_pairs"]) for s in stats)
     Pf = sum(int(s["n_cluster_points"]) for s in stats)
     Cp = sum(int(s["n_peak_clusters"]) for s in stats)
     return {
         "threshold": 2 * N,                     # read grey, write thresholded
-        "ccl_local": N + 2 * N + 4 * N,         # read thr, write parents (2 slots / 4 px) and tile counts
-        "ccl_border": 0,
-        "ccl_final": 2 * N + 4 * N + 4 * N,     # read parents, write labels and sizes
-        "boundaries_pairs": 4 * N + 4 * N + 8 * P,  # labels, size gathers, tagged points
+        "ccl_local": N + 8 * N,                 # read thresholded; write 4 scratch + 4 size words per 2x2 block
+        "ccl_border": 0,                        # latency: a few unions per tile edge
+        "ccl_final": 5 * N + 8 * N,             # read parents, sizes, pixels; write parents, sizes, labels
+        "boundaries_pairs": 4 * N + 8 * Pf,     # read labels; write the listed points (>= surviving ones)
         "pairs_finalize": 48 * C,
-        "scatter_points": 8 * P + 8 * Pf,
+        "scatter_points": 8 * Pf + 8 * Pf,      # read listed points, write sort keys
         "cluster_sort": (8 + 4 + 8 + 64) * Pf,  # keys, grey taps, ClusterPoints, prefix sums
         "cluster_errors": 48 * Pf,              # each prefix sum read once
-        "index_quads": Cp * (120 + 210 * 8 * 48 + 272),
+        "index_quads": Cp * (120 + 90 * 2 * 48 + 272),
     }
 
 
