@@ -231,8 +231,6 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     const int bx = bx0 + tx, by = by0 + ty;
     const bool live = bx < w / 2 && by < h / 2;
     const uint32_t l = threadIdx.x;
-    par[2 * l] = 2 * l;
-    par[2 * l + 1] = 2 * l + 1;
     cnt[2 * l] = 0;
     cnt[2 * l + 1] = 0;
     __syncthreads();
@@ -241,15 +239,43 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     if (live) {
         const int r0 = 2 * ty + 1, c0 = 2 * tx + 1;
         L = block_links([&](int dy, int dx) { return (uint32_t)pix[r0 + dy][c0 + dx]; }, bx * 2, by * 2, w, h);
-        // intra-tile links
-        const int ndx[4] = {-1, 0, 1, -1}, ndy[4] = {-1, -1, -1, 0};
-#pragma unroll
-        for (int n = 0; n < 4; n++) {
-            int ntxl = tx + ndx[n], ntyl = ty + ndy[n];
-            if (ntxl < 0 || ntxl >= CCL_BX || ntyl < 0) continue;
-            uint32_t nl = ntyl * CCL_BX + ntxl;
-            if (L.wmask & (1u << n)) uf_union((volatile uint32_t*)par, 2 * l, 2 * nl);
-            if (L.bmask & (1u << n)) uf_union((volatile uint32_t*)par, 2 * l + 1, 2 * nl + 1);
+    }
+    // S links (left neighbour) inside the tile row, which is this warp: a run
+    // of blocks that each link to their left neighbour points at its first
+    // block, a smaller slot, so the root of a set stays its minimum
+    const uint32_t lane = (uint32_t)tx;
+    const unsigned sw = __ballot_sync(0xFFFFFFFFu, live && tx > 0 && (L.wmask & 8u));
+    const unsigned sb = __ballot_sync(0xFFFFFFFFu, live && tx > 0 && (L.bmask & 8u));
+    {
+        const unsigned le = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+        const uint32_t row0 = (uint32_t)ty * CCL_BX;
+        par[2 * l] = 2 * (row0 + 31 - __clz(~sw & le));
+        par[2 * l + 1] = 2 * (row0 + 31 - __clz(~sb & le)) + 1;
+    }
+    __syncthreads();
+    // P, Q, R links (up-left, up, up-right) inside the tile.  Within a run,
+    // the block above-left of lane i is the block above lane i - 1: the P
+    // link of i is left out when i - 1 is in the same run and has its Q
+    // link (the same union), and likewise R against i + 1
+    if (ty > 0) {
+        const unsigned qw = __ballot_sync(0xFFFFFFFFu, live && (L.wmask & 2u));
+        const unsigned qb = __ballot_sync(0xFFFFFFFFu, live && (L.bmask & 2u));
+        if (live) {
+            const uint32_t up = l - CCL_BX;
+            const bool skip_pw = ((sw >> lane) & 1u) && ((qw >> (lane - 1)) & 1u);
+            const bool skip_pb = ((sb >> lane) & 1u) && ((qb >> (lane - 1)) & 1u);
+            const bool skip_rw = lane < 31 && ((sw >> (lane + 1)) & 1u) && ((qw >> (lane + 1)) & 1u);
+            const bool skip_rb = lane < 31 && ((sb >> (lane + 1)) & 1u) && ((qb >> (lane + 1)) & 1u);
+            if (L.wmask & 2u) uf_union((volatile uint32_t*)par, 2 * l, 2 * up);
+            if (L.bmask & 2u) uf_union((volatile uint32_t*)par, 2 * l + 1, 2 * up + 1);
+            if (tx > 0) {
+                if ((L.wmask & 1u) && !skip_pw) uf_union((volatile uint32_t*)par, 2 * l, 2 * (up - 1));
+                if ((L.bmask & 1u) && !skip_pb) uf_union((volatile uint32_t*)par, 2 * l + 1, 2 * (up - 1) + 1);
+            }
+            if (tx < CCL_BX - 1) {
+                if ((L.wmask & 4u) && !skip_rw) uf_union((volatile uint32_t*)par, 2 * l, 2 * (up + 1));
+                if ((L.bmask & 4u) && !skip_rb) uf_union((volatile uint32_t*)par, 2 * l + 1, 2 * (up + 1) + 1);
+            }
         }
     }
     __syncthreads();
