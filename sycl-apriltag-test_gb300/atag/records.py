@@ -63,7 +63,8 @@ class Tuning(ctypes.Structure):
     """atag_tuning: launch shapes of the detector's kernels."""
     _fields_ = [("ccl_tile_rows", ctypes.c_int32), ("boundary_tile_rows", ctypes.c_int32),
                 ("small_cluster_max", ctypes.c_int32), ("small_ctas_per_sm", ctypes.c_int32),
-                ("large_ctas_divisor", ctypes.c_int32), ("index_ctas_per_sm", ctypes.c_int32)]
+                ("large_ctas_divisor", ctypes.c_int32), ("index_ctas_per_sm", ctypes.c_int32),
+                ("batch_lanes", ctypes.c_int32)]
 
     def as_dict(self):
         return {n: int(getattr(self, n)) for n, _ in self._fields_}

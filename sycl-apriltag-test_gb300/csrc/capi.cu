@@ -197,6 +197,7 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, FrameDe
 
 constexpr int RING = 16;
 constexpr size_t WORK_LISTS = 5;  // batch-wide work lists of the per-cluster kernels
+constexpr int MAX_LANES = 2;      // sub-batches of one call that run concurrently
 
 }  // namespace
 
@@ -218,9 +219,11 @@ struct atag_detector {
     bool owns_ws = false;
     // header carve-out
     FrameDesc* d_tables = nullptr;   // RING x max_frames
-    uint32_t* d_work = nullptr;      // offsets (WORK_LISTS x (max_frames + 1)) + WORK_LISTS counters
-    cudaStream_t side = nullptr;     // second stream for the large-cluster kernel
-    cudaEvent_t fork = nullptr, join = nullptr;
+    uint32_t* d_work = nullptr;      // per lane: offsets (WORK_LISTS x (max_frames + 1)) + WORK_LISTS counters
+    cudaStream_t lane_stream = nullptr;          // stream of the second sub-batch
+    cudaStream_t side[MAX_LANES] = {};           // per lane: stream of the large-cluster kernel
+    cudaEvent_t fork[MAX_LANES] = {}, join[MAX_LANES] = {};
+    cudaEvent_t lane_fork = nullptr, lane_join = nullptr;
     uint8_t* d_input = nullptr;      // host-upload input region
     size_t input_bytes = 0;
     atag_quad_corners* d_hquads = nullptr;  // host-path quad staging
@@ -236,7 +239,7 @@ struct atag_detector {
     std::vector<FrameDesc> last;     // table last uploaded
     std::vector<FrameDesc> cur;      // table of the last call
     std::vector<cudaEvent_t> stage_events;
-    atag_tuning tuning{16, 16, (int32_t)CF_SMALL_CAP, 8, 2, 8};
+    atag_tuning tuning{16, 16, (int32_t)CF_SMALL_CAP, 8, 2, 8, 2};
 };
 
 namespace {
@@ -246,7 +249,7 @@ constexpr size_t HOST_QUAD_CAP = 4096;
 size_t header_bytes(size_t max_frames, size_t input_bytes) {
     size_t b = 0;
     b += al(sizeof(FrameDesc) * RING * max_frames);
-    b += al(4 * (WORK_LISTS * (max_frames + 1) + WORK_LISTS));
+    b += al(4 * MAX_LANES * (WORK_LISTS * (max_frames + 1) + WORK_LISTS));
     b += al(input_bytes);
     b += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
     b += al(sizeof(atag_frame_stats));
@@ -482,7 +485,7 @@ atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t ma
     }
     char* p = det->ws;
     det->d_tables = (FrameDesc*)p; p += al(sizeof(FrameDesc) * RING * max_frames);
-    det->d_work = (uint32_t*)p; p += al(4 * (WORK_LISTS * (max_frames + 1) + WORK_LISTS));
+    det->d_work = (uint32_t*)p; p += al(4 * MAX_LANES * (WORK_LISTS * (max_frames + 1) + WORK_LISTS));
     det->input_bytes = max_total_pixels * (size_t)c.decimate * (size_t)c.decimate;
     det->d_input = (uint8_t*)p; p += al(det->input_bytes);
     det->d_hquads = (atag_quad_corners*)p; p += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
@@ -497,9 +500,14 @@ atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t ma
         return fail(ATAG_ERR_OUT_OF_MEMORY, "cudaHostAlloc: %s", cudaGetErrorString(e));
     }
     for (int i = 0; i < RING; i++) cudaEventCreateWithFlags(&det->ev[i], cudaEventDisableTiming);
-    cudaStreamCreateWithFlags(&det->side, cudaStreamNonBlocking);
-    cudaEventCreateWithFlags(&det->fork, cudaEventDisableTiming);
-    cudaEventCreateWithFlags(&det->join, cudaEventDisableTiming);
+    for (int k = 0; k < MAX_LANES; k++) {
+        cudaStreamCreateWithFlags(&det->side[k], cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&det->fork[k], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&det->join[k], cudaEventDisableTiming);
+    }
+    cudaStreamCreateWithFlags(&det->lane_stream, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&det->lane_fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&det->lane_join, cudaEventDisableTiming);
     *out = det;
     return ATAG_OK;
 }
@@ -510,12 +518,20 @@ atag_status atag_detector_destroy(atag_detector* det) {
         cudaEventSynchronize(det->ev[i]);
         cudaEventDestroy(det->ev[i]);
     }
-    if (det->side) {
-        cudaStreamSynchronize(det->side);
-        cudaStreamDestroy(det->side);
+    for (int k = 0; k < MAX_LANES; k++) {
+        if (det->side[k]) {
+            cudaStreamSynchronize(det->side[k]);
+            cudaStreamDestroy(det->side[k]);
+        }
+        if (det->fork[k]) cudaEventDestroy(det->fork[k]);
+        if (det->join[k]) cudaEventDestroy(det->join[k]);
     }
-    if (det->fork) cudaEventDestroy(det->fork);
-    if (det->join) cudaEventDestroy(det->join);
+    if (det->lane_stream) {
+        cudaStreamSynchronize(det->lane_stream);
+        cudaStreamDestroy(det->lane_stream);
+    }
+    if (det->lane_fork) cudaEventDestroy(det->lane_fork);
+    if (det->lane_join) cudaEventDestroy(det->lane_join);
     if (det->h_staging) cudaFreeHost(det->h_staging);
     if (det->owns_ws) cudaFree(det->ws);
     delete det;
@@ -543,57 +559,36 @@ static atag_status upload_table(atag_detector* det, const std::vector<FrameDesc>
     return ATAG_OK;
 }
 
-atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size_t n, atag_quad_corners* d_quads,
-                              size_t quad_cap, atag_frame_stats* d_stats, atag_stream_t stream) {
-    if (!det || !frames || n == 0 || !d_quads || !d_stats) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: bad argument");
-    if (n > det->max_frames) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: %zu frames > max %zu", n, det->max_frames);
-    cudaStream_t s = (cudaStream_t)stream;
-    const uint32_t f = (uint32_t)det->cfg.decimate;
-    std::vector<FrameDesc> t(n);
-    size_t off = 0, total_px = 0, mw = 0, mh = 0, max_pair = 0, max_points = 0;
-    bool any_decim = f > 1;
-    for (size_t i = 0; i < n; i++) {
-        const atag_frame& fr = frames[i];
-        if (!fr.d_grey) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu has no image", i);
-        size_t w = fr.src_width / f, h = fr.src_height / f;
-        if (!valid_dims(w, h) || w > det->max_w || h > det->max_h)
-            return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu is %ux%u; after decimation by %u it must be a multiple of 4 within %zux%zu",
-                        i, fr.src_width, fr.src_height, f, det->max_w, det->max_h);
-        total_px += w * h;
-        if (total_px > det->max_total_pixels) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: batch exceeds %zu pixels", det->max_total_pixels);
-        size_t bytes = layout_frame(det->frames_base + off, (uint32_t)w, (uint32_t)h, f, &t[i]);
-        off += bytes;
-        if (off > det->frames_bytes) return fail(ATAG_ERR_OUT_OF_MEMORY, "detect_batch: workspace too small");
-        FrameDesc& d = t[i];
-        d.src = fr.d_grey;
-        d.src_stride = fr.src_width;
-        if (f == 1) d.grey = const_cast<uint8_t*>(fr.d_grey);
-        d.quads = d_quads + i * quad_cap;
-        d.quad_cap = (uint32_t)quad_cap;
-        d.stats = d_stats + i;
-        mw = std::max(mw, w); mh = std::max(mh, h);
-        max_pair = std::max<size_t>(max_pair, d.pair_cap);
-        max_points = std::max<size_t>(max_points, d.point_cap);
+// The whole path for frames [first, last) of the uploaded table, on stream
+// s, with lane `lane`'s work lists and side stream.  Stage events are
+// recorded when `timed`.
+static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, const std::vector<FrameDesc>& t,
+                               size_t first, size_t last, cudaStream_t s, int lane, bool timed) {
+    const size_t n = last - first;
+    size_t mw = 0, mh = 0, max_pair = 0, max_points = 0;
+    bool any_decim = false;
+    for (size_t i = first; i < last; i++) {
+        mw = std::max<size_t>(mw, t[i].width);
+        mh = std::max<size_t>(mh, t[i].height);
+        max_pair = std::max<size_t>(max_pair, t[i].pair_cap);
+        max_points = std::max<size_t>(max_points, t[i].point_cap);
+        any_decim |= t[i].factor > 1;
     }
-    const FrameDesc* d_table;
-    atag_status st = upload_table(det, t, s, &d_table);
-    if (st) return st;
-    det->cur = t;
     FrameSet fs;
     memset(&fs, 0, sizeof fs);
-    fs.table = d_table;
+    fs.table = d_table + first;
     const PipelineParams& p = det->pp;
     const int sms = det->dev->num_sms;
-    // batch-wide work lists: small clusters, large clusters, point runs,
-    // all clusters, clusters with peaks; one queue cursor each
-    uint32_t* off_small = det->d_work;
-    uint32_t* off_large = det->d_work + (n + 1);
-    uint32_t* off_runs = det->d_work + 2 * (n + 1);
-    uint32_t* off_clusters = det->d_work + 3 * (n + 1);
-    uint32_t* off_peaks = det->d_work + 4 * (n + 1);
-    uint32_t* wc = det->d_work + WORK_LISTS * (det->max_frames + 1);
-
-    const bool timed = det->stage_events.size() == ATAG_STAGE_COUNT + 1;
+    // batch-wide work lists of this lane: small clusters, large clusters,
+    // point runs, all clusters, clusters with peaks; one queue cursor each
+    uint32_t* work = det->d_work + (size_t)lane * (WORK_LISTS * (det->max_frames + 1) + WORK_LISTS);
+    uint32_t* off_small = work;
+    uint32_t* off_large = work + (n + 1);
+    uint32_t* off_runs = work + 2 * (n + 1);
+    uint32_t* off_clusters = work + 3 * (n + 1);
+    uint32_t* off_peaks = work + 4 * (n + 1);
+    uint32_t* wc = work + WORK_LISTS * (det->max_frames + 1);
+    cudaStream_t side = det->side[lane];
     auto mark = [&](int i) -> atag_status {
         if (timed) CK(cudaEventRecord(det->stage_events[i], s));
         return ATAG_OK;
@@ -648,10 +643,10 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     LAUNCHED();
     STAGE(9);
     // large clusters on the side stream, concurrently with the small ones
-    CK(cudaEventRecord(det->fork, s));
-    CK(cudaStreamWaitEvent(det->side, det->fork, 0));
+    CK(cudaEventRecord(det->fork[lane], s));
+    CK(cudaStreamWaitEvent(side, det->fork[lane], 0));
     k_cluster_sort_large<<<std::max(1, sms / std::max(1, tu.large_ctas_divisor)), CF_LARGE_THREADS, CF_LARGE_SMEM,
-                           det->side>>>(fs, off_large, (uint32_t)n, wc + 1);
+                           side>>>(fs, off_large, (uint32_t)n, wc + 1);
     LAUNCHED();
     {
         // the small-cluster kernel's key buffers are sized for the tuned split
@@ -661,8 +656,8 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
             fs, off_small, (uint32_t)n, wc, cap);
     }
     LAUNCHED();
-    CK(cudaEventRecord(det->join, det->side));
-    CK(cudaStreamWaitEvent(s, det->join, 0));
+    CK(cudaEventRecord(det->join[lane], side));
+    CK(cudaStreamWaitEvent(s, det->join[lane], 0));
     STAGE(10);
     k_cluster_errors<<<sms * 8, 256, 0, s>>>(fs, off_runs, (uint32_t)n, wc + 2);
     LAUNCHED();
@@ -685,6 +680,64 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     LAUNCHED();
     STAGE(15);
 #undef STAGE
+    return ATAG_OK;
+}
+
+atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size_t n, atag_quad_corners* d_quads,
+                              size_t quad_cap, atag_frame_stats* d_stats, atag_stream_t stream) {
+    if (!det || !frames || n == 0 || !d_quads || !d_stats) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: bad argument");
+    if (n > det->max_frames) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: %zu frames > max %zu", n, det->max_frames);
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t f = (uint32_t)det->cfg.decimate;
+    std::vector<FrameDesc> t(n);
+    size_t off = 0, total_px = 0;
+    for (size_t i = 0; i < n; i++) {
+        const atag_frame& fr = frames[i];
+        if (!fr.d_grey) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu has no image", i);
+        size_t w = fr.src_width / f, h = fr.src_height / f;
+        if (!valid_dims(w, h) || w > det->max_w || h > det->max_h)
+            return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu is %ux%u; after decimation by %u it must be a multiple of 4 within %zux%zu",
+                        i, fr.src_width, fr.src_height, f, det->max_w, det->max_h);
+        total_px += w * h;
+        if (total_px > det->max_total_pixels) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: batch exceeds %zu pixels", det->max_total_pixels);
+        size_t bytes = layout_frame(det->frames_base + off, (uint32_t)w, (uint32_t)h, f, &t[i]);
+        off += bytes;
+        if (off > det->frames_bytes) return fail(ATAG_ERR_OUT_OF_MEMORY, "detect_batch: workspace too small");
+        FrameDesc& d = t[i];
+        d.src = fr.d_grey;
+        d.src_stride = fr.src_width;
+        if (f == 1) d.grey = const_cast<uint8_t*>(fr.d_grey);
+        d.quads = d_quads + i * quad_cap;
+        d.quad_cap = (uint32_t)quad_cap;
+        d.stats = d_stats + i;
+    }
+    const FrameDesc* d_table;
+    atag_status st = upload_table(det, t, s, &d_table);
+    if (st) return st;
+    det->cur = t;
+    // Two lanes: the batch is split into two halves by pixel count that run
+    // concurrently on two streams (one graph when captured), so each half's
+    // serial kernels and tails overlap the other half's work.  Stage timing
+    // needs one stream, so it runs one lane.
+    const bool timed = det->stage_events.size() == ATAG_STAGE_COUNT + 1;
+    const int lanes = (timed || n < 2) ? 1 : std::min(det->tuning.batch_lanes, MAX_LANES);
+    if (lanes == 1) return launch_lane(det, d_table, t, 0, n, s, 0, timed);
+    size_t split = n / 2, acc = 0;
+    for (size_t i = 0; i < n; i++) {
+        acc += (size_t)t[i].width * t[i].height;
+        if (2 * acc >= total_px) {
+            split = std::min<size_t>(i + 1, n - 1);
+            break;
+        }
+    }
+    CK(cudaEventRecord(det->lane_fork, s));
+    CK(cudaStreamWaitEvent(det->lane_stream, det->lane_fork, 0));
+    st = launch_lane(det, d_table, t, 0, split, s, 0, false);
+    if (st) return st;
+    st = launch_lane(det, d_table, t, split, n, det->lane_stream, 1, false);
+    if (st) return st;
+    CK(cudaEventRecord(det->lane_join, det->lane_stream));
+    CK(cudaStreamWaitEvent(s, det->lane_join, 0));
     return ATAG_OK;
 }
 
@@ -766,6 +819,8 @@ atag_status atag_detector_set_tuning(atag_detector* det, const atag_tuning* t) {
     if (t->small_ctas_per_sm < 1 || t->small_ctas_per_sm > 16 || t->large_ctas_divisor < 1 ||
         t->large_ctas_divisor > 64 || t->index_ctas_per_sm < 1 || t->index_ctas_per_sm > 64)
         return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: CTA counts out of range");
+    if (t->batch_lanes < 1 || t->batch_lanes > MAX_LANES)
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: batch_lanes must be in [1, %d]", MAX_LANES);
     det->tuning = *t;
     return ATAG_OK;
 }

@@ -145,9 +145,9 @@ def test_every_tuning_gives_identical_results_and_autotune_applies(tmp_path):
     det = Detector(1920, 1080, max_frames=2, max_total_pixels=sum(i.size for i in imgs))
     base, _ = det.detect(frames)
     for t in ({"ccl_tile_rows": 8, "boundary_tile_rows": 8, "small_cluster_max": 1024, "small_ctas_per_sm": 2,
-               "large_ctas_divisor": 8, "index_ctas_per_sm": 4},
+               "large_ctas_divisor": 8, "index_ctas_per_sm": 4, "batch_lanes": 1},
               {"ccl_tile_rows": 16, "boundary_tile_rows": 8, "small_cluster_max": 2048, "small_ctas_per_sm": 6,
-               "large_ctas_divisor": 2, "index_ctas_per_sm": 16}):
+               "large_ctas_divisor": 2, "index_ctas_per_sm": 16, "batch_lanes": 2}):
         det.set_tuning(**t)
         q, st = det.detect(frames)
         for a, b in zip(q, base):
