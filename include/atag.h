@@ -363,7 +363,7 @@ typedef struct atag_tuning {
     int32_t large_ctas_divisor;   /* large-cluster CTAs = SMs / divisor (2)         */
     int32_t index_ctas_per_sm;    /* CTAs of the combination search per SM (8)      */
     int32_t batch_lanes;          /* a batch runs as this many sub-batches on
-                                     concurrent streams (1..2, default 2)           */
+                                     concurrent streams (1..4, default 2)           */
 } atag_tuning;
 
 atag_status atag_detector_get_tuning(const atag_detector *det, atag_tuning *out);

@@ -197,7 +197,7 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, FrameDe
 
 constexpr int RING = 16;
 constexpr size_t WORK_LISTS = 5;  // batch-wide work lists of the per-cluster kernels
-constexpr int MAX_LANES = 2;      // sub-batches of one call that run concurrently
+constexpr int MAX_LANES = 4;      // sub-batches of one call that run concurrently
 
 }  // namespace
 
@@ -220,10 +220,10 @@ struct atag_detector {
     // header carve-out
     FrameDesc* d_tables = nullptr;   // RING x max_frames
     uint32_t* d_work = nullptr;      // per lane: offsets (WORK_LISTS x (max_frames + 1)) + WORK_LISTS counters
-    cudaStream_t lane_stream = nullptr;          // stream of the second sub-batch
+    cudaStream_t lane_stream[MAX_LANES] = {};    // streams of lanes 1.. (lane 0 runs on the caller's)
     cudaStream_t side[MAX_LANES] = {};           // per lane: stream of the large-cluster kernel
     cudaEvent_t fork[MAX_LANES] = {}, join[MAX_LANES] = {};
-    cudaEvent_t lane_fork = nullptr, lane_join = nullptr;
+    cudaEvent_t lane_fork = nullptr, lane_join[MAX_LANES] = {};
     uint8_t* d_input = nullptr;      // host-upload input region
     size_t input_bytes = 0;
     atag_quad_corners* d_hquads = nullptr;  // host-path quad staging
@@ -505,9 +505,11 @@ atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t ma
         cudaEventCreateWithFlags(&det->fork[k], cudaEventDisableTiming);
         cudaEventCreateWithFlags(&det->join[k], cudaEventDisableTiming);
     }
-    cudaStreamCreateWithFlags(&det->lane_stream, cudaStreamNonBlocking);
+    for (int k = 1; k < MAX_LANES; k++) {
+        cudaStreamCreateWithFlags(&det->lane_stream[k], cudaStreamNonBlocking);
+        cudaEventCreateWithFlags(&det->lane_join[k], cudaEventDisableTiming);
+    }
     cudaEventCreateWithFlags(&det->lane_fork, cudaEventDisableTiming);
-    cudaEventCreateWithFlags(&det->lane_join, cudaEventDisableTiming);
     *out = det;
     return ATAG_OK;
 }
@@ -526,12 +528,14 @@ atag_status atag_detector_destroy(atag_detector* det) {
         if (det->fork[k]) cudaEventDestroy(det->fork[k]);
         if (det->join[k]) cudaEventDestroy(det->join[k]);
     }
-    if (det->lane_stream) {
-        cudaStreamSynchronize(det->lane_stream);
-        cudaStreamDestroy(det->lane_stream);
+    for (int k = 1; k < MAX_LANES; k++) {
+        if (det->lane_stream[k]) {
+            cudaStreamSynchronize(det->lane_stream[k]);
+            cudaStreamDestroy(det->lane_stream[k]);
+        }
+        if (det->lane_join[k]) cudaEventDestroy(det->lane_join[k]);
     }
     if (det->lane_fork) cudaEventDestroy(det->lane_fork);
-    if (det->lane_join) cudaEventDestroy(det->lane_join);
     if (det->h_staging) cudaFreeHost(det->h_staging);
     if (det->owns_ws) cudaFree(det->ws);
     delete det;
@@ -715,29 +719,42 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     atag_status st = upload_table(det, t, s, &d_table);
     if (st) return st;
     det->cur = t;
-    // Two lanes: the batch is split into two halves by pixel count that run
-    // concurrently on two streams (one graph when captured), so each half's
-    // serial kernels and tails overlap the other half's work.  Stage timing
-    // needs one stream, so it runs one lane.
+    // Lanes: the batch is split into up to MAX_LANES parts of about equal
+    // pixel count that run the whole path concurrently on their own streams
+    // (branches of one graph when captured), so each part's serial kernels
+    // and tails overlap the other parts' work.  Stage timing needs one
+    // stream, so it runs one lane.
     const bool timed = det->stage_events.size() == ATAG_STAGE_COUNT + 1;
-    const int lanes = (timed || n < 2) ? 1 : std::min(det->tuning.batch_lanes, MAX_LANES);
+    const int lanes = timed ? 1 : (int)std::min<size_t>((size_t)std::min(det->tuning.batch_lanes, MAX_LANES), n);
     if (lanes == 1) return launch_lane(det, d_table, t, 0, n, s, 0, timed);
-    size_t split = n / 2, acc = 0;
-    for (size_t i = 0; i < n; i++) {
-        acc += (size_t)t[i].width * t[i].height;
-        if (2 * acc >= total_px) {
-            split = std::min<size_t>(i + 1, n - 1);
-            break;
+    size_t cut[MAX_LANES + 1];
+    cut[0] = 0;
+    cut[lanes] = n;
+    {
+        size_t acc = 0, i = 0;
+        for (int k = 1; k < lanes; k++) {
+            // first frame index whose prefix reaches k/lanes of the pixels,
+            // leaving at least one frame for each later lane
+            while (i < n && acc * lanes < total_px * (size_t)k) {
+                acc += (size_t)t[i].width * t[i].height;
+                i++;
+            }
+            cut[k] = std::min(std::max(i, cut[k - 1] + 1), n - (size_t)(lanes - k));
+            i = cut[k];
+            acc = 0;
+            for (size_t j = 0; j < i; j++) acc += (size_t)t[j].width * t[j].height;
         }
     }
     CK(cudaEventRecord(det->lane_fork, s));
-    CK(cudaStreamWaitEvent(det->lane_stream, det->lane_fork, 0));
-    st = launch_lane(det, d_table, t, 0, split, s, 0, false);
-    if (st) return st;
-    st = launch_lane(det, d_table, t, split, n, det->lane_stream, 1, false);
-    if (st) return st;
-    CK(cudaEventRecord(det->lane_join, det->lane_stream));
-    CK(cudaStreamWaitEvent(s, det->lane_join, 0));
+    for (int k = 1; k < lanes; k++) CK(cudaStreamWaitEvent(det->lane_stream[k], det->lane_fork, 0));
+    for (int k = 0; k < lanes; k++) {
+        st = launch_lane(det, d_table, t, cut[k], cut[k + 1], k ? det->lane_stream[k] : s, k, false);
+        if (st) return st;
+    }
+    for (int k = 1; k < lanes; k++) {
+        CK(cudaEventRecord(det->lane_join[k], det->lane_stream[k]));
+        CK(cudaStreamWaitEvent(s, det->lane_join[k], 0));
+    }
     return ATAG_OK;
 }
 

@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(256) k_reset_frames(const __grid_constant__ Fr
 // ---------------------------------------------------------------------------
 constexpr int BP_W = 64;                       // tile width; BP_H (8 or 16) rows is a tuning choice
 constexpr int BP_SW = BP_W + 2;
-constexpr int BP_LC = 256;                     // CTA hash-table entries
+constexpr int BP_LC = 128;                     // CTA hash-table entries (a tile has a few dozen pairs)
+constexpr uint32_t BP_BIG = 0x40000000u, BP_VALUE = 0x3FFFFFFFu;
 
 struct PairTableSmem {
     unsigned long long key[BP_LC];
@@ -139,8 +140,9 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     const int x0 = (blockIdx.x % ntx) * BP_W, y0 = (blockIdx.x / ntx) * BP_H;
     uint32_t* status = F.counters + CNT_STATUS;
 
+    // labels of the tile and its halo; bit 30 (free: label values are
+    // below 2^24) marks a component of at least min_size pixels
     __shared__ uint32_t lab[BP_SH][BP_SW];
-    __shared__ uint8_t big[BP_SH][BP_SW];
     __shared__ PairTableSmem T;
     __shared__ uint32_t stage[BP_STAGE];
     __shared__ uint32_t red[33];
@@ -162,8 +164,8 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         for (int k = 0; k < NL; k++) {
             const int i = threadIdx.x + k * THREADS, r = i / BP_SW, c = i % BP_SW;
             if (i < BP_SH * BP_SW) {
-                lab[r][c] = lv[k];
-                big[r][c] = __ldg(F.sizes + (lv[k] & LABEL_VALUE_MASK)) >= min_size;
+                const bool big = __ldg(F.sizes + (lv[k] & LABEL_VALUE_MASK)) >= min_size;
+                lab[r][c] = lv[k] | (big ? BP_BIG : 0u);
             }
         }
     }
@@ -186,15 +188,15 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         const int xo = cbase + k, x = x0 + xo, c = xo + 1;
-        if (!(y < h && x > 0 && x < w) || !big[r][c]) continue;
+        if (!(y < h && x > 0 && x < w) || !(lab[r][c] & BP_BIG)) continue;
         const uint32_t cp = lab[r][c] & LABEL_PIXEL_MASK;
         const bool dup = (lab[r][c - 1] & LABEL_PIXEL_MASK) != (lab[r + 1][c] & LABEL_PIXEL_MASK) &&
-                         big[r][c - 1] && big[r + 1][c];
+                         (lab[r][c - 1] & BP_BIG) && (lab[r + 1][c] & BP_BIG);
         uint32_t m = 0;
-        m |= ((lab[r][c + 1] & LABEL_PIXEL_MASK) != cp && big[r][c + 1]) ? 1u : 0u;
-        m |= (!dup && (lab[r + 1][c - 1] & LABEL_PIXEL_MASK) != cp && big[r + 1][c - 1]) ? 2u : 0u;
-        m |= ((lab[r + 1][c] & LABEL_PIXEL_MASK) != cp && big[r + 1][c]) ? 4u : 0u;
-        m |= ((lab[r + 1][c + 1] & LABEL_PIXEL_MASK) != cp && big[r + 1][c + 1]) ? 8u : 0u;
+        m |= ((lab[r][c + 1] & LABEL_PIXEL_MASK) != cp && (lab[r][c + 1] & BP_BIG)) ? 1u : 0u;
+        m |= (!dup && (lab[r + 1][c - 1] & LABEL_PIXEL_MASK) != cp && (lab[r + 1][c - 1] & BP_BIG)) ? 2u : 0u;
+        m |= ((lab[r + 1][c] & LABEL_PIXEL_MASK) != cp && (lab[r + 1][c] & BP_BIG)) ? 4u : 0u;
+        m |= ((lab[r + 1][c + 1] & LABEL_PIXEL_MASK) != cp && (lab[r + 1][c + 1] & BP_BIG)) ? 8u : 0u;
         masks |= m << (4 * k);
     }
     uint32_t nst;
@@ -207,7 +209,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
             const int xo = cbase + k, x = x0 + xo, c = xo + 1;
             const int rr = r + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
             const uint32_t p = lab[r][c], q = lab[rr][cc];
-            const uint32_t lp = p & LABEL_VALUE_MASK, lq = q & LABEL_VALUE_MASK;
+            const uint32_t lp = p & BP_VALUE, lq = q & BP_VALUE;
             const int dir = (q & LABEL_PIXEL_MASK) > (p & LABEL_PIXEL_MASK) ? 1 : 0;
             const unsigned long long key = ((unsigned long long)min(lp, lq) << 32) | max(lp, lq);
             int ls;
@@ -603,9 +605,9 @@ __device__ __forceinline__ void cluster_sort(const FrameSet& fs, const uint32_t*
         const unsigned long long* src = F.sortbuf + start;
         if (n <= sort_cap) {
             if (LARGE) {
-                if (n <= THREADS * 8) sort_keys_regs<THREADS, 8>(src, n, X);
-                else if (n <= THREADS * 16) sort_keys_regs<THREADS, 16>(src, n, X);
-                else sort_keys_regs<THREADS, 32>(src, n, X);
+                if (n <= THREADS * 4) sort_keys_regs<THREADS, 4>(src, n, X);
+                else if (n <= THREADS * 8) sort_keys_regs<THREADS, 8>(src, n, X);
+                else sort_keys_regs<THREADS, 16>(src, n, X);
             } else {
                 if (n <= THREADS * 2) sort_keys_regs<THREADS, 2>(src, n, X);
                 else if (n <= THREADS * 4) sort_keys_regs<THREADS, 4>(src, n, X);
@@ -914,11 +916,11 @@ __global__ void __launch_bounds__(1024) k_compact_quads(const __grid_constant__ 
     }
 }
 
-__global__ void __launch_bounds__(BP_W / 4 * 8) k_boundaries_pairs_r8(const __grid_constant__ FrameSet fs,
+__global__ void __launch_bounds__(BP_W / 4 * 8, 16) k_boundaries_pairs_r8(const __grid_constant__ FrameSet fs,
                                                                        uint32_t min_size) {
     boundaries_pairs_impl<8>(fs, min_size);
 }
-__global__ void __launch_bounds__(BP_W / 4 * 16) k_boundaries_pairs_r16(const __grid_constant__ FrameSet fs,
+__global__ void __launch_bounds__(BP_W / 4 * 16, 8) k_boundaries_pairs_r16(const __grid_constant__ FrameSet fs,
                                                                         uint32_t min_size) {
     boundaries_pairs_impl<16>(fs, min_size);
 }
