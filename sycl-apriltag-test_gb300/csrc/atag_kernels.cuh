@@ -90,12 +90,12 @@ enum Counter : uint32_t {
 };
 
 // Cluster-sort kernel shapes: most clusters are small and run several per SM
-// on 128 threads (up to 16 keys per thread), large ones get a 1024-thread
-// CTA (up to 16 keys per thread); both sort in registers with a shared-memory
+// on 128 threads (up to 16 keys per thread), large ones get a 512-thread CTA
+// (up to 32 keys per thread); both sort in registers with a shared-memory
 // exchange buffer of CF_*_CAP keys.  Clusters larger than CF_LARGE_CAP (4K
 // frames only) radix-sort in global memory with per-warp counters.
 constexpr uint32_t CF_SMALL_THREADS = 128, CF_SMALL_CAP = CF_SMALL_THREADS * 16;
-constexpr uint32_t CF_LARGE_THREADS = 1024, CF_LARGE_CAP = CF_LARGE_THREADS * 16;
+constexpr uint32_t CF_LARGE_THREADS = 512, CF_LARGE_CAP = CF_LARGE_THREADS * 32;
 constexpr uint32_t CF_SMALL_SMEM = CF_SMALL_CAP * 8;
 constexpr uint32_t CF_LARGE_SMEM = CF_LARGE_CAP * 8 + (CF_LARGE_THREADS / 32) * 256 * 4;
 // Window errors / filter / peaks: one warp per run of up to CE_RUN

@@ -605,9 +605,9 @@ __device__ __forceinline__ void cluster_sort(const FrameSet& fs, const uint32_t*
         const unsigned long long* src = F.sortbuf + start;
         if (n <= sort_cap) {
             if (LARGE) {
-                if (n <= THREADS * 4) sort_keys_regs<THREADS, 4>(src, n, X);
-                else if (n <= THREADS * 8) sort_keys_regs<THREADS, 8>(src, n, X);
-                else sort_keys_regs<THREADS, 16>(src, n, X);
+                if (n <= THREADS * 8) sort_keys_regs<THREADS, 8>(src, n, X);
+                else if (n <= THREADS * 16) sort_keys_regs<THREADS, 16>(src, n, X);
+                else sort_keys_regs<THREADS, 32>(src, n, X);
             } else {
                 if (n <= THREADS * 2) sort_keys_regs<THREADS, 2>(src, n, X);
                 else if (n <= THREADS * 4) sort_keys_regs<THREADS, 4>(src, n, X);
