@@ -2,7 +2,7 @@
 """Benchmark: 1080p AprilTag quad detection frames/s on GB300.
 
 One step = one batched detection (atag_detect_batch, replayed as a CUDA
-graph) over a batch of seeded synthetic 1920x1080 frames (40 fiducials,
+graph) over a batch of 64 seeded synthetic 1920x1080 frames (40 fiducials,
 300 clutter shapes, blur and noise: the reference has no dataset), inputs
 resident in HBM.  Also measured:
   plain   single-frame path, one graph replay per frame, L2 flushed before
@@ -231,7 +231,7 @@ def main():
                     "long enough for several clock samples)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--batch", type=int, default=64, help="frames per step (64, as in the batching configuration)")
     ap.add_argument("--decimate", type=int, default=1)
     ap.add_argument("--plain-frames", type=int, default=64)
     ap.add_argument("--cpu-sample", type=int, default=32)
