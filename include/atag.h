@@ -175,6 +175,26 @@ uint64_t atag_launch_count(void);
 atag_status atag_decimate(const uint8_t *d_src, size_t src_width, size_t src_height,
                           size_t factor, uint8_t *d_dst, atag_stream_t stream);
 
+/* Input pixel formats.  Colour is removed the way the reference's loader
+ * does it (stbi_load(..., STBI_grey), src/main.cpp:264-265): luma
+ * (77 r + 150 g + 29 b) >> 8, alpha ignored (include/stb_image.h:1834-1836);
+ * grey + alpha keeps the grey byte.  Planar YUV inputs pass their Y plane
+ * as ATAG_PIX_GREY8. */
+typedef enum atag_pixel_format {
+    ATAG_PIX_GREY8 = 0,
+    ATAG_PIX_RGB8 = 1,
+    ATAG_PIX_RGBA8 = 2,
+    ATAG_PIX_BGR8 = 3,
+    ATAG_PIX_BGRA8 = 4,
+    ATAG_PIX_GREYA8 = 5
+} atag_pixel_format;
+
+/* Colour removal and point-sampling decimation in one pass (notes.txt
+ * steps 1-2): dst(x,y) = grey(src(f*x, f*y)); src rows are src_pitch bytes
+ * apart (0 = width * bytes per pixel). */
+atag_status atag_convert_grey(const uint8_t *d_src, size_t src_width, size_t src_height, size_t src_pitch,
+                              int format, size_t factor, uint8_t *d_dst, atag_stream_t stream);
+
 /* Replaces threshold_image (include/threshold.h:6-10, src/threshold.cpp:3-98).
  * d_extrema / d_filtered_extrema are 2 bytes per 4x4 tile (min, max) and may
  * be NULL: the fused kernel keeps them in shared memory and only writes them
@@ -246,10 +266,15 @@ atag_status atag_process_fitted_quads(const atag_fitted_quad *d_fitted, size_t f
 /* ------------------------------------------------------------------ */
 typedef struct atag_detector atag_detector;
 
-/* One frame of a batch.  d_grey is the source image before decimation. */
+/* One frame of a batch: the source image before colour removal and
+ * decimation, `format` an atag_pixel_format (0: grey), rows src_pitch
+ * bytes apart (0: packed).  A zero-initialised tail means a packed grey
+ * image. */
 typedef struct atag_frame {
     const uint8_t *d_grey;
     uint32_t src_width, src_height;
+    uint32_t format;
+    uint32_t src_pitch;
 } atag_frame;
 
 /* Bytes of device workspace a detector needs for up to max_frames frames

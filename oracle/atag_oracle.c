@@ -296,6 +296,39 @@ void oracle_decimate(const uint8_t *src, int src_w, int src_h, int f, uint8_t *d
         for (int x = 0; x < w; x++) dst[(size_t)y * w + x] = src[(size_t)y * f * src_w + (size_t)x * f];
 }
 
+/* Colour removal (notes.txt step 1).  The reference removes colour when it
+ * loads its input: stbi_load(..., STBI_grey) (src/main.cpp:264-265), i.e.
+ * stb's luma y = (77 r + 150 g + 29 b) >> 8 for 3 and 4 channels, alpha
+ * ignored (include/stb_image.h:1834-1836, 1899-1915), and the grey channel
+ * of grey + alpha.  BGR orders swap r and b. */
+static int pixel_bytes(int format) {
+    switch (format) {
+    case ATAG_PIX_GREY8: return 1;
+    case ATAG_PIX_GREYA8: return 2;
+    case ATAG_PIX_RGB8: case ATAG_PIX_BGR8: return 3;
+    case ATAG_PIX_RGBA8: case ATAG_PIX_BGRA8: return 4;
+    }
+    return 0;
+}
+static uint8_t luma(int r, int g, int b) { return (uint8_t)((r * 77 + g * 150 + b * 29) >> 8); }
+
+void oracle_to_grey(const uint8_t *src, int src_w, int src_h, int src_pitch, int format, int f, uint8_t *dst) {
+    const int bpp = pixel_bytes(format);
+    const size_t pitch = src_pitch ? (size_t)src_pitch : (size_t)src_w * bpp;
+    const int w = src_w / f, h = src_h / f;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const uint8_t *p = src + (size_t)y * f * pitch + (size_t)x * f * bpp;
+            uint8_t v;
+            switch (format) {
+            case ATAG_PIX_RGB8: case ATAG_PIX_RGBA8: v = luma(p[0], p[1], p[2]); break;
+            case ATAG_PIX_BGR8: case ATAG_PIX_BGRA8: v = luma(p[2], p[1], p[0]); break;
+            default: v = p[0]; break; /* grey, grey + alpha */
+            }
+            dst[(size_t)y * w + x] = v;
+        }
+}
+
 /* ------------------------------------------------------------------ */
 /* Stage a1: threshold.cpp:8-95                                       */
 /* ------------------------------------------------------------------ */

@@ -79,6 +79,11 @@ float oracle_hypotf(float a, float b);
 
 /* --- stages --- */
 void oracle_decimate(const uint8_t *src, int src_w, int src_h, int factor, uint8_t *dst);
+/* Colour removal + decimation: pixel (f x, f y) of a src_w x src_h image of
+ * `format` (ATAG_PIX_*, include/atag.h) with rows src_pitch bytes apart (0 =
+ * packed), to one grey byte; dst is (src_w / f) x (src_h / f). */
+void oracle_to_grey(const uint8_t *src, int src_w, int src_h, int src_pitch, int format, int factor,
+                    uint8_t *dst);
 void oracle_threshold(const uint8_t *grey, int w, int h, int min_white_black_diff,
                       uint8_t *extrema, uint8_t *filtered, uint8_t *out);
 /* scratch may be NULL (then allocated internally); labels/sizes w*h. */

@@ -80,6 +80,7 @@ def lib():
         L.oracle_segmentation.argtypes = [_P, ctypes.c_int, ctypes.c_int, _P, _P, _P]
         L.oracle_find_boundaries.argtypes = [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P]
         L.oracle_decimate.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
+        L.oracle_to_grey.argtypes = [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P]
         L.oracle_fit_lines_windowed.argtypes = [_P, _P, _P, _SZ, _P]
         L.oracle_fit_lines_cyclic.argtypes = [_P, _P, _P, _SZ, _P]
         L.oracle_do_indexing.argtypes = [_P, _SZ, _P, _P, _P, ctypes.POINTER(Config), _P]
@@ -183,6 +184,17 @@ def find_boundaries(labels: np.ndarray, sizes: np.ndarray, min_size: int = 25):
     keys = np.full(4 * w * h, np.uint64(0xFFFFFFFFFFFFFFFF), np.uint64)
     lib().oracle_find_boundaries(_ptr(lab), _ptr(s), w, h, min_size, _ptr(pts), _ptr(keys))
     return pts, keys
+
+
+def to_grey(src: np.ndarray, factor: int = 1, fmt: int = None) -> np.ndarray:
+    """Colour removal + decimation (oracle_to_grey): src H x W or H x W x C."""
+    src = np.ascontiguousarray(src, dtype=np.uint8)
+    h, w = src.shape[0], src.shape[1]
+    if fmt is None:
+        fmt = 0 if src.ndim == 2 else {1: 0, 2: 5, 3: 1, 4: 2}[src.shape[2]]
+    out = np.empty((h // factor, w // factor), np.uint8)
+    lib().oracle_to_grey(_ptr(src), w, h, 0, fmt, factor, _ptr(out))
+    return out
 
 
 def decimate(src: np.ndarray, factor: int):

@@ -7,7 +7,15 @@ import torch
 
 from . import lib
 from .records import (CLUSTER_BOUNDS, CLUSTER_EXTENTS, CLUSTER_POINT, CORNER, FITTED_QUAD, FRAME_STATS,
-                      LINE_FIT_POINT, PEAK_EXTENTS, QUAD_CORNERS, Frame, FrameViews)
+                      LINE_FIT_POINT, PEAK_EXTENTS, PIX_GREY8, PIX_GREYA8, PIX_RGB8, PIX_RGBA8, PIXEL_BYTES,
+                      QUAD_CORNERS, Frame, FrameViews)
+
+
+def frame_format(t):
+    """atag_pixel_format implied by a frame tensor's shape."""
+    if t.dim() == 2:
+        return PIX_GREY8
+    return {1: PIX_GREY8, 2: PIX_GREYA8, 3: PIX_RGB8, 4: PIX_RGBA8}[t.shape[2]]
 
 _P = ctypes.c_void_p
 
@@ -51,17 +59,23 @@ class Detector:
         except Exception:
             pass
 
-    def enqueue(self, frames, stream=None):
-        """Launches detection of `frames` (uint8 CUDA tensors, H x W, before
-        decimation) on `stream` (default: torch's current stream)."""
+    def enqueue(self, frames, stream=None, formats=None):
+        """Launches detection of `frames` (uint8 CUDA tensors before colour
+        removal and decimation: H x W grey, or H x W x C with C = 2 grey +
+        alpha, 3 RGB, 4 RGBA) on `stream` (default: torch's current stream).
+        `formats` (one atag_pixel_format per frame) overrides the format
+        implied by the shape, e.g. for BGR."""
         frames = [f if f.is_contiguous() else f.contiguous() for f in frames]
         n = len(frames)
         arr = (Frame * n)()
         for i, f in enumerate(frames):
-            assert f.dtype == torch.uint8 and f.is_cuda and f.dim() == 2
+            assert f.dtype == torch.uint8 and f.is_cuda and f.dim() in (2, 3)
+            fmt = formats[i] if formats is not None else frame_format(f)
             arr[i].d_grey = f.data_ptr()
             arr[i].src_width = f.shape[1]
             arr[i].src_height = f.shape[0]
+            arr[i].format = fmt
+            arr[i].src_pitch = f.shape[1] * PIXEL_BYTES[fmt]
         s = stream if stream is not None else torch.cuda.current_stream()
         lib.check(self.L.atag_detect_batch(self.handle, arr, n, _P(self.d_quads.data_ptr()), self.quad_capacity,
                                            _P(self.d_stats.data_ptr()), _P(s.cuda_stream)), "atag_detect_batch")
@@ -78,8 +92,8 @@ class Detector:
         q = q.reshape(self._n, self.quad_capacity)
         return [q[i, : int(st[i]["n_quads"])].copy() for i in range(self._n)], st
 
-    def detect(self, frames):
-        self.enqueue(frames)
+    def detect(self, frames, formats=None):
+        self.enqueue(frames, formats=formats)
         return self.results()
 
     def detect_host(self, image: np.ndarray, stream=None):

@@ -31,6 +31,7 @@ _SIGNATURES = {
     "atag_use_device": (_ST, [ctypes.c_int]),
     "atag_launch_count": (ctypes.c_uint64, []),
     "atag_decimate": (_ST, [_P, _SZ, _SZ, _SZ, _P, _P]),
+    "atag_convert_grey": (_ST, [_P, _SZ, _SZ, _SZ, ctypes.c_int, _SZ, _P, _P]),
     "atag_threshold_image": (_ST, [_P, _P, _P, _P, _SZ, _SZ, _P]),
     "atag_image_segmentation": (_ST, [_P, _P, _P, _P, _SZ, _SZ, _SZ, _P]),
     "atag_image_segmentation_noalloc": (_ST, [_P, _P, _P, _SZ, _SZ, _P]),

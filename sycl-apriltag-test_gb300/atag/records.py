@@ -38,8 +38,14 @@ class Config(ctypes.Structure):
                 ("compat_peak_index", ctypes.c_int32)]
 
 
+# atag_pixel_format (include/atag.h)
+PIX_GREY8, PIX_RGB8, PIX_RGBA8, PIX_BGR8, PIX_BGRA8, PIX_GREYA8 = range(6)
+PIXEL_BYTES = {PIX_GREY8: 1, PIX_RGB8: 3, PIX_RGBA8: 4, PIX_BGR8: 3, PIX_BGRA8: 4, PIX_GREYA8: 2}
+
+
 class Frame(ctypes.Structure):
-    _fields_ = [("d_grey", ctypes.c_void_p), ("src_width", ctypes.c_uint32), ("src_height", ctypes.c_uint32)]
+    _fields_ = [("d_grey", ctypes.c_void_p), ("src_width", ctypes.c_uint32), ("src_height", ctypes.c_uint32),
+                ("format", ctypes.c_uint32), ("src_pitch", ctypes.c_uint32)]
 
 
 class FrameViews(ctypes.Structure):

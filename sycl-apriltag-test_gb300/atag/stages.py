@@ -43,6 +43,21 @@ def decimate(src: torch.Tensor, factor: int) -> torch.Tensor:
     return out
 
 
+def convert_grey(src: torch.Tensor, factor: int = 1, fmt: int = None) -> torch.Tensor:
+    """Colour removal + decimation (atag_convert_grey): src is H x W (grey)
+    or H x W x C (C = 2, 3, 4: grey + alpha, RGB, RGBA; `fmt` for BGR)."""
+    from .detector import frame_format
+    from .records import PIXEL_BYTES
+    L = lib.init()
+    src = src.contiguous()
+    h, w = src.shape[0], src.shape[1]
+    fmt = frame_format(src) if fmt is None else fmt
+    out = torch.empty((h // factor, w // factor), dtype=torch.uint8, device=src.device)
+    lib.check(L.atag_convert_grey(_ptr(src), w, h, w * PIXEL_BYTES[fmt], fmt, factor, _ptr(out), _stream()),
+              "atag_convert_grey")
+    return out
+
+
 def threshold_image(grey: torch.Tensor, with_extrema: bool = False):
     """threshold_image (include/threshold.h:6-10): returns the {0,127,255}
     image, and the tile extrema (min, max) before and after dilation when

@@ -178,6 +178,17 @@ __host__ __device__ __forceinline__ float hypot_f(float a, float b) {
     return u2f((uint32_t)(k + 23 + 127) << 23 | ((uint32_t)q & 0x7FFFFFu));
 }
 
+// bytes per pixel of an atag_pixel_format (0 for an unknown format)
+__host__ __device__ __forceinline__ uint32_t pixel_bytes(uint32_t format) {
+    switch (format) {
+    case ATAG_PIX_GREY8: return 1;
+    case ATAG_PIX_GREYA8: return 2;
+    case ATAG_PIX_RGB8: case ATAG_PIX_BGR8: return 3;
+    case ATAG_PIX_RGBA8: case ATAG_PIX_BGRA8: return 4;
+    default: return 0;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // BoundaryPoint helpers (boundary_point.h).  COORDINATE_HALF_PIXEL_MASK is 0
 // (boundary_point.h:16), so dx() == 1 and dy() == 0 for every point.

@@ -14,9 +14,10 @@ struct FrameDesc {
     uint32_t width, height;            // after decimation
     uint32_t factor;                   // decimation factor
     uint32_t src_stride;               // source row pitch in bytes
+    uint32_t src_format;               // atag_pixel_format of the source
     // pixel buffers
     const uint8_t* src;                // source frame (before decimation)
-    uint8_t* grey;                     // decimated frame (== src when factor 1)
+    uint8_t* grey;                     // decimated grey frame (== src when grey and factor 1)
     uint8_t* thr;                      // thresholded
     uint8_t* extrema;                  // optional tile min/max (2 B / tile)
     uint8_t* filtered_extrema;         // optional dilated min/max

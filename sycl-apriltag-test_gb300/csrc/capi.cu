@@ -143,7 +143,8 @@ FrameCaps caps_for(size_t N) {
 
 // Lays out one frame's buffers at `base` (device address, may be 0 to only
 // measure).  Returns the bytes used.
-size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, FrameDesc* d) {
+// own_grey: the frame needs its own grey buffer (decimated or colour input)
+size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, bool own_grey, FrameDesc* d) {
     size_t N = (size_t)w * h;
     FrameCaps c = caps_for(N);
     size_t off = 0;
@@ -156,7 +157,7 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, FrameDe
     f.width = w;
     f.height = h;
     f.factor = factor;
-    f.grey = factor > 1 ? (uint8_t*)take(N) : nullptr;
+    f.grey = own_grey ? (uint8_t*)take(N) : nullptr;
     f.thr = (uint8_t*)take(N);
     f.scratch = (uint32_t*)take(4 * N);
     f.labels = (uint32_t*)take(4 * N);
@@ -258,9 +259,9 @@ size_t header_bytes(size_t max_frames, size_t input_bytes) {
 
 size_t frames_bound(size_t max_frames, size_t max_total_pixels) {
     // bytes(N) is bounded by a per-frame constant plus a per-pixel slope
-    size_t c0 = layout_frame(nullptr, 4, 4, 2, nullptr);
+    size_t c0 = layout_frame(nullptr, 4, 4, 2, true, nullptr);
     size_t big = 1 << 22;  // 4 Mpx
-    size_t cb = layout_frame(nullptr, 2048, 2048, 2, nullptr);
+    size_t cb = layout_frame(nullptr, 2048, 2048, 2, true, nullptr);
     double slope = (double)(cb) / (double)big;
     return max_frames * (c0 + 64 * ALIGN) + (size_t)(slope * 1.25 * (double)max_total_pixels) + (1 << 20);
 }
@@ -320,7 +321,33 @@ atag_status atag_decimate(const uint8_t* src, size_t sw, size_t sh, size_t f, ui
     }
     FrameDesc d = blank();
     d.width = (uint32_t)w; d.height = (uint32_t)h; d.factor = (uint32_t)f; d.src_stride = (uint32_t)sw;
+    d.src_format = ATAG_PIX_GREY8;
     d.src = src; d.grey = dst;
+    k_decimate<<<grid2(std::min<size_t>(cdiv(w / 4 * h, 256), 4096), 1), 256, 0, (cudaStream_t)stream>>>(single(d));
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+atag_status atag_convert_grey(const uint8_t* src, size_t sw, size_t sh, size_t pitch, int format, size_t f,
+                              uint8_t* dst, atag_stream_t stream) {
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    const uint32_t bpp = format < 0 ? 0u : pixel_bytes((uint32_t)format);
+    if (!src || !dst || f < 1 || f > 64 || bpp == 0)
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "convert_grey: bad pointer, factor or pixel format");
+    if (pitch == 0) pitch = sw * bpp;
+    if (pitch < sw * bpp) return fail(ATAG_ERR_INVALID_ARGUMENT, "convert_grey: row pitch below the width");
+    size_t w = sw / f, h = sh / f;
+    if (!valid_dims(w, h)) return fail(ATAG_ERR_INVALID_ARGUMENT, "convert_grey: %zux%zu after decimation is not a multiple of 4 in [4, 4096]", w, h);
+    FrameDesc d = blank();
+    d.width = (uint32_t)w; d.height = (uint32_t)h; d.factor = (uint32_t)f; d.src_stride = (uint32_t)pitch;
+    d.src_format = (uint32_t)format;
+    d.src = src; d.grey = dst;
+    if (f == 1 && format == ATAG_PIX_GREY8) {
+        CK(cudaMemcpy2DAsync(dst, w, src, pitch, w, h, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+        return ATAG_OK;
+    }
     k_decimate<<<grid2(std::min<size_t>(cdiv(w / 4 * h, 256), 4096), 1), 256, 0, (cudaStream_t)stream>>>(single(d));
     LAUNCHED();
     return ATAG_OK;
@@ -576,7 +603,7 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
         mh = std::max<size_t>(mh, t[i].height);
         max_pair = std::max<size_t>(max_pair, t[i].pair_cap);
         max_points = std::max<size_t>(max_points, t[i].point_cap);
-        any_decim |= t[i].factor > 1;
+        any_decim |= t[i].factor > 1 || t[i].src_format != ATAG_PIX_GREY8;
     }
     FrameSet fs;
     memset(&fs, 0, sizeof fs);
@@ -698,19 +725,26 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
     for (size_t i = 0; i < n; i++) {
         const atag_frame& fr = frames[i];
         if (!fr.d_grey) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu has no image", i);
+        const uint32_t bpp = pixel_bytes(fr.format);
+        if (bpp == 0) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu has unknown pixel format %u", i, fr.format);
+        const size_t pitch = fr.src_pitch ? fr.src_pitch : (size_t)fr.src_width * bpp;
+        if (pitch < (size_t)fr.src_width * bpp)
+            return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu has a row pitch below its width", i);
         size_t w = fr.src_width / f, h = fr.src_height / f;
         if (!valid_dims(w, h) || w > det->max_w || h > det->max_h)
             return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: frame %zu is %ux%u; after decimation by %u it must be a multiple of 4 within %zux%zu",
                         i, fr.src_width, fr.src_height, f, det->max_w, det->max_h);
         total_px += w * h;
         if (total_px > det->max_total_pixels) return fail(ATAG_ERR_INVALID_ARGUMENT, "detect_batch: batch exceeds %zu pixels", det->max_total_pixels);
-        size_t bytes = layout_frame(det->frames_base + off, (uint32_t)w, (uint32_t)h, f, &t[i]);
+        const bool convert = f > 1 || fr.format != ATAG_PIX_GREY8;
+        size_t bytes = layout_frame(det->frames_base + off, (uint32_t)w, (uint32_t)h, f, convert, &t[i]);
         off += bytes;
         if (off > det->frames_bytes) return fail(ATAG_ERR_OUT_OF_MEMORY, "detect_batch: workspace too small");
         FrameDesc& d = t[i];
         d.src = fr.d_grey;
-        d.src_stride = fr.src_width;
-        if (f == 1) d.grey = const_cast<uint8_t*>(fr.d_grey);
+        d.src_stride = (uint32_t)pitch;
+        d.src_format = fr.format;
+        if (!convert) d.grey = const_cast<uint8_t*>(fr.d_grey);
         d.quads = d_quads + i * quad_cap;
         d.quad_cap = (uint32_t)quad_cap;
         d.stats = d_stats + i;

@@ -8,19 +8,35 @@
 namespace atag {
 
 // ---------------------------------------------------------------------------
-// a0: point-sampling decimation dst(x, y) = src(f x, f y)
+// a0: colour removal and point-sampling decimation dst(x, y) = grey(src(f x,
+// f y)).  Colour is removed the way the reference's loader does it,
+// stbi_load(..., STBI_grey) (src/main.cpp:264-265): luma (77 r + 150 g +
+// 29 b) >> 8 with alpha ignored (include/stb_image.h:1834-1836); grey + alpha
+// keeps the grey byte.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pixel_grey(const uint8_t* p, uint32_t format) {
+    switch (format) {
+    case ATAG_PIX_RGB8: case ATAG_PIX_RGBA8:
+        return ((uint32_t)p[0] * 77u + (uint32_t)p[1] * 150u + (uint32_t)p[2] * 29u) >> 8;
+    case ATAG_PIX_BGR8: case ATAG_PIX_BGRA8:
+        return ((uint32_t)p[2] * 77u + (uint32_t)p[1] * 150u + (uint32_t)p[0] * 29u) >> 8;
+    default: return p[0];
+    }
+}
+
 __global__ void k_decimate(const __grid_constant__ FrameSet fs) {
     const FrameDesc& F = fs.get(blockIdx.y);
-    if (F.factor <= 1) return;
-    const uint32_t w = F.width, h = F.height, f = F.factor;
+    if (F.factor <= 1 && F.src_format == ATAG_PIX_GREY8) return;
+    const uint32_t w = F.width, h = F.height, f = F.factor, fmt = F.src_format;
+    const uint32_t bpp = pixel_bytes(fmt);
     const uint32_t words_per_row = w / 4;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < words_per_row * h;
          i += gridDim.x * blockDim.x) {
-        uint32_t y = i / words_per_row, xw = i % words_per_row;
-        const uint8_t* s = F.src + (size_t)y * f * F.src_stride + (size_t)xw * 4 * f;
-        uint32_t v = (uint32_t)s[0] | ((uint32_t)s[f] << 8) | ((uint32_t)s[2 * f] << 16) |
-                     ((uint32_t)s[3 * f] << 24);
+        const uint32_t y = i / words_per_row, xw = i % words_per_row;
+        const uint8_t* s = F.src + (size_t)y * f * F.src_stride + (size_t)xw * 4 * f * bpp;
+        uint32_t v = 0;
+#pragma unroll
+        for (int b = 0; b < 4; b++) v |= pixel_grey(s + (size_t)b * f * bpp, fmt) << (8 * b);
         reinterpret_cast<uint32_t*>(F.grey)[(size_t)y * words_per_row + xw] = v;
     }
 }

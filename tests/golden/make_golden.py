@@ -13,6 +13,10 @@ Writes:
                         seeded inputs
   pipeline.json         per frame and per stage: element count and SHA-256 of
                         the canonical bytes (record padding excluded)
+  colour.npz            colour removal as the reference's loader does it: seeded
+                        grey + alpha, RGB and RGBA images encoded with the
+                        reference's vendored stb_image_write.h and decoded with
+                        its stb_image.h to one channel (oracle/_ref/stb_grey)
 """
 import hashlib
 import json
@@ -56,6 +60,29 @@ def small_frames():
     return out
 
 
+def colour_cases():
+    """Seeded 2/3/4-channel images: uniform noise, and a synthetic frame
+    tinted per channel (so the luma weights matter)."""
+    from atag import synth
+    rng = np.random.default_rng(11)
+    out = {}
+    for c in (2, 3, 4):
+        out[f"noise_c{c}"] = rng.integers(0, 256, (48, 64, c), dtype=np.uint8)
+    grey = synth.render(synth.CONFIGS["vga"], 4)[100:220, 200:360].astype(np.int32)
+    for c in (3, 4):
+        chans = [np.clip(grey * rng.uniform(0.6, 1.2) + rng.integers(-40, 40), 0, 255) for _ in range(c)]
+        out[f"tinted_c{c}"] = np.stack(chans, axis=-1).astype(np.uint8)
+    return out
+
+
+def run_stb_grey(tool, img, tmp):
+    h, w, c = img.shape
+    np.ascontiguousarray(img).tofile(os.path.join(tmp, "c.raw"))
+    subprocess.run([tool, os.path.join(tmp, "c.raw"), str(w), str(h), str(c), os.path.join(tmp, "g.raw")],
+                   check=True, capture_output=True)
+    return np.fromfile(os.path.join(tmp, "g.raw"), dtype=np.uint8).reshape(h, w)
+
+
 def run_pipeline(harness, img, tmp):
     img.tofile(os.path.join(tmp, "in.raw"))
     subprocess.run([harness, os.path.join(tmp, "in.raw"), str(img.shape[1]), str(img.shape[0]), tmp], check=True,
@@ -86,6 +113,13 @@ def main():
         rec = {name: np.fromfile(os.path.join(tmp, name + ".bin"), dtype=dt)
                for name, dt in golden_io.RECORD_ARRAYS.items()}
     np.savez_compressed(os.path.join(HERE, "records.npz"), **rec)
+    stb = build_refshim.build_stb_grey()
+    colour = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for name, img in colour_cases().items():
+            colour[name] = img
+            colour[name + "_grey"] = run_stb_grey(stb, img, tmp)
+    np.savez_compressed(os.path.join(HERE, "colour.npz"), **colour)
     with open(os.path.join(HERE, "pipeline.json"), "w") as f:
         json.dump(pipeline, f, indent=1, sort_keys=True)
     print("golden vectors written:", ", ".join(sorted(pipeline)))

@@ -95,3 +95,23 @@ def test_get_moment_cyclic_ranges(records):
     out, cnt = oracle.eval_get_moment(records["rec_prefix"], records["rec_moment_range"])
     assert golden_io.digest(out) == golden_io.digest(records["rec_moment"])
     assert np.array_equal(cnt, records["rec_moment_n"])
+
+
+def test_colour_removal_matches_the_reference_loader():
+    """oracle.to_grey against the reference's own colour removal: stb's
+    STBI_grey decode of the same pixels (tests/golden/colour.npz); BGR
+    orders are the RGB images with the channels reversed."""
+    with np.load(os.path.join(GOLDEN, "colour.npz")) as z:
+        cases = {k: z[k] for k in z.files}
+    names = [k for k in cases if not k.endswith("_grey")]
+    assert len(names) >= 5
+    for name in names:
+        img, want = cases[name], cases[name + "_grey"]
+        assert np.array_equal(oracle.to_grey(img), want), name
+        c = img.shape[2]
+        if c in (3, 4):
+            bgr = img.copy()
+            bgr[..., [0, 2]] = img[..., [2, 0]]
+            assert np.array_equal(oracle.to_grey(bgr, fmt=3 if c == 3 else 4), want), name
+        # decimation samples the same pixels
+        assert np.array_equal(oracle.to_grey(img, factor=2), want[::2, ::2][: img.shape[0] // 2, : img.shape[1] // 2])
