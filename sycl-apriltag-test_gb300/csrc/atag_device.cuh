@@ -576,14 +576,12 @@ __device__ __forceinline__ uint32_t block_exclusive_scan_u32(uint32_t v, uint32_
     return r;
 }
 
-// Stable LSD radix sort of n 64-bit keys for a CTA of THREADS threads, 8
-// bits per pass.  Each warp owns a contiguous range of the input so the
-// scatter keeps input order within a digit; passes where every key has the
-// same digit are skipped.  `hist` holds THREADS/32 x 256 counters, `red` 33
-// slots.  Returns the buffer that holds the sorted keys (a or b).  (Sorting
-// on the theta half alone and ordering ties afterwards does not pay: theta
-// carries a quadrant offset of 2^16, so it has 7 fractional bits there and
-// long runs of equal values.)
+// Shared-memory key arrays of the cluster sorts keep one spare slot after
+// every 16 keys: a warp whose lanes touch 2 to 16 consecutive keys each
+// (sorted runs, per-lane segments) then hits distinct banks.
+__host__ __device__ constexpr uint32_t kpad(uint32_t i) { return i + (i >> 4); }
+__host__ __device__ constexpr uint32_t kpad_size(uint32_t n) { return n + n / 16; }
+
 // ---------------------------------------------------------------------------
 // Bitonic sort of T*K 64-bit keys held K per thread in registers.  On exit
 // thread t holds elements [t K, t K + K) of the ascending order.  Element e
@@ -646,8 +644,9 @@ __device__ __forceinline__ void bitonic_sort_regs(unsigned long long (&v)[K], un
     }
 }
 
-// Sorts src[0, n) (global memory, n <= T*K) into dst[0, n) (shared memory of
-// T*K keys, also used for the exchange); all threads of the CTA call it.
+// Sorts src[0, n) (global memory, n <= T*K) into dst[kpad(i)] (shared memory
+// of kpad_size(T*K) keys, also used for the exchange); all threads of the
+// CTA call it.
 template <int T, int K>
 __device__ __forceinline__ void sort_keys_regs(const unsigned long long* __restrict__ src, uint32_t n,
                                                unsigned long long* dst) {
@@ -663,8 +662,76 @@ __device__ __forceinline__ void sort_keys_regs(const unsigned long long* __restr
 #pragma unroll
     for (int r = 0; r < K; r++) {
         const uint32_t e = threadIdx.x * K + r;
-        if (e < n) dst[e] = v[r];
+        if (e < n) dst[kpad(e)] = v[r];
     }
+    __syncthreads();
+}
+
+// Block merge sort of src[0, n) (global memory, n <= T*K) into dst[kpad(i)]
+// (shared memory of kpad_size(T*K) keys).  Each thread sorts K keys in
+// registers, then log2(T) rounds merge pairs of sorted runs, doubling their
+// length: a thread finds where its K outputs start on the merge path of its
+// two runs (binary search along the diagonal, ties taken from the first
+// run) and merges K keys serially.  Its work is O(n log(n / K)) against the
+// O(n log^2 n) of a bitonic network, which pays from about 8 keys per thread.
+template <int T, int K>
+__device__ __forceinline__ void merge_sort_keys(const unsigned long long* __restrict__ src, uint32_t n,
+                                                unsigned long long* dst) {
+    static_assert(K >= 2 && K <= 32 && (K & (K - 1)) == 0, "K must be a power of two in [2, 32]");
+    unsigned long long v[K];
+#pragma unroll
+    for (int r = 0; r < K; r++) {
+        const uint32_t e = (uint32_t)(r * T) + threadIdx.x;  // coalesced; the order is sorted away
+        v[r] = e < n ? src[e] : ~0ull;
+    }
+#pragma unroll
+    for (int k = 2; k <= K; k <<= 1)
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+            for (int r = 0; r < K; r++) {
+                const int p = r ^ j;
+                if (p > r) {
+                    const unsigned long long a = v[r], b = v[p];
+                    const bool sw = (a > b) == ((r & k) == 0);
+                    v[r] = sw ? b : a;
+                    v[p] = sw ? a : b;
+                }
+            }
+    const uint32_t tid = threadIdx.x;
+#pragma unroll 1
+    for (uint32_t width = 1; width < (uint32_t)T; width <<= 1) {
+#pragma unroll
+        for (int r = 0; r < K; r++) dst[kpad(tid * K + r)] = v[r];
+        __syncthreads();
+        const uint32_t g0 = tid & ~(2 * width - 1), L = width * K;
+        const uint32_t a0 = g0 * K, b0 = a0 + L, d = (tid - g0) * K;
+        uint32_t lo = d > L ? d - L : 0u, hi = d < L ? d : L;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (dst[kpad(a0 + mid)] <= dst[kpad(b0 + d - 1 - mid)]) lo = mid + 1;
+            else hi = mid;
+        }
+        uint32_t i = lo, j = d - lo;
+        unsigned long long a = i < L ? dst[kpad(a0 + i)] : 0ull;
+        unsigned long long b = j < L ? dst[kpad(b0 + j)] : 0ull;
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const bool ta = j >= L || (i < L && a <= b);
+            v[k] = ta ? a : b;
+            if (k + 1 < K) {
+                i += ta ? 1u : 0u;
+                j += ta ? 0u : 1u;
+                const uint32_t ni = ta ? i : j;
+                const unsigned long long nv = ni < L ? dst[kpad((ta ? a0 : b0) + ni)] : 0ull;
+                a = ta ? nv : a;
+                b = ta ? b : nv;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < K; r++) dst[kpad(tid * K + r)] = v[r];
     __syncthreads();
 }
 
@@ -682,6 +749,14 @@ __device__ __forceinline__ unsigned match_digit8(uint32_t d, bool valid) {
     return m;
 }
 
+// Stable LSD radix sort of n 64-bit keys for a CTA of THREADS threads, 8
+// bits per pass.  Each warp owns a contiguous range of the input so the
+// scatter keeps input order within a digit; passes where every key has the
+// same digit are skipped.  `hist` holds THREADS/32 x 256 counters, `red` 33
+// slots.  Returns the buffer that holds the sorted keys (a or b).  (Sorting
+// on the theta half alone and ordering ties afterwards does not pay: theta
+// carries a quadrant offset of 2^16, so it has 7 fractional bits there and
+// long runs of equal values.)
 template <uint32_t THREADS>
 __device__ __forceinline__ unsigned long long* block_radix_sort_u64(unsigned long long* a, unsigned long long* b,
                                                                    uint32_t n, uint32_t* hist, uint32_t* red,

@@ -92,13 +92,21 @@ enum Counter : uint32_t {
 
 // Cluster-sort kernel shapes: most clusters are small and run several per SM
 // on 128 threads (up to 16 keys per thread), large ones get a 512-thread CTA
-// (up to 32 keys per thread); both sort in registers with a shared-memory
-// exchange buffer of CF_*_CAP keys.  Clusters larger than CF_LARGE_CAP (4K
-// frames only) radix-sort in global memory with per-warp counters.
+// (up to 32 keys per thread); both sort in registers and shared memory (a
+// padded array of kpad_size(cap) keys).  Clusters larger than CF_LARGE_CAP
+// (4K frames only) radix-sort in global memory with per-warp counters.
 constexpr uint32_t CF_SMALL_THREADS = 128, CF_SMALL_CAP = CF_SMALL_THREADS * 16;
 constexpr uint32_t CF_LARGE_THREADS = 512, CF_LARGE_CAP = CF_LARGE_THREADS * 32;
-constexpr uint32_t CF_SMALL_SMEM = CF_SMALL_CAP * 8;
-constexpr uint32_t CF_LARGE_SMEM = CF_LARGE_CAP * 8 + (CF_LARGE_THREADS / 32) * 256 * 4;
+constexpr uint32_t CF_SMALL_SMEM = kpad_size(CF_SMALL_CAP) * 8;
+constexpr uint32_t CF_LARGE_SMEM = kpad_size(CF_LARGE_CAP) * 8 + (CF_LARGE_THREADS / 32) * 256 * 4;
+// Shared memory of the small-cluster kernel for clusters of at most `cap`
+// points: the sorts work on whole powers of two of at least 2 keys per
+// thread.
+__host__ __device__ constexpr uint32_t cf_small_smem(uint32_t cap) {
+    uint32_t k = CF_SMALL_THREADS * 2;
+    while (k < cap) k <<= 1;
+    return kpad_size(k) * 8;
+}
 // Window errors / filter / peaks: one warp per run of up to CE_RUN
 // consecutive points of one cluster.
 constexpr uint32_t CE_RUN = 256;

@@ -682,7 +682,7 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
     {
         // the small-cluster kernel's key buffers are sized for the tuned split
         const uint32_t cap = (uint32_t)tu.small_cluster_max;
-        const uint32_t smem = cap * 8;
+        const uint32_t smem = cf_small_smem(cap);
         k_cluster_sort_small<<<sms * std::max(1, tu.small_ctas_per_sm), CF_SMALL_THREADS, smem, s>>>(
             fs, off_small, (uint32_t)n, wc, cap);
     }

@@ -488,55 +488,6 @@ __global__ void __launch_bounds__(256) k_scatter_points(const __grid_constant__ 
 // inputs and their prefix sums
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ long long shfl_up_ll(long long v, int o) {
-    return (long long)__shfl_up_sync(0xffffffffu, (unsigned long long)v, o);
-}
-
-// Block-wide exclusive scan of 6 int64 lanes; returns the thread's prefix.
-__device__ __forceinline__ Moment block_exclusive_scan_moment(const Moment& v, long long (*red)[6]) {
-    long long x[6] = {v.Mx, v.My, v.Mxx, v.Myy, v.Mxy, v.W};
-    long long incl[6];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-    for (int j = 0; j < 6; j++) {
-        long long s = x[j];
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            long long y = shfl_up_ll(s, o);
-            if (lane >= o) s = wadd(s, y);
-        }
-        incl[j] = s;
-    }
-    __syncthreads();
-    if (lane == 31) {
-#pragma unroll
-        for (int j = 0; j < 6; j++) red[wid][j] = incl[j];
-    }
-    __syncthreads();
-    if (wid == 0) {
-#pragma unroll
-        for (int j = 0; j < 6; j++) {
-            long long t = lane < nw ? red[lane][j] : 0;
-            long long s = t;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                long long y = shfl_up_ll(s, o);
-                if (lane >= o) s = wadd(s, y);
-            }
-            if (lane < nw) red[lane][j] = wsub(s, t);  // exclusive warp offsets
-        }
-    }
-    __syncthreads();
-    Moment r;
-    r.Mx = wadd(red[wid][0], wsub(incl[0], x[0]));
-    r.My = wadd(red[wid][1], wsub(incl[1], x[1]));
-    r.Mxx = wadd(red[wid][2], wsub(incl[2], x[2]));
-    r.Myy = wadd(red[wid][3], wsub(incl[3], x[3]));
-    r.Mxy = wadd(red[wid][4], wsub(incl[4], x[4]));
-    r.W = wadd(red[wid][5], wsub(incl[5], x[5]));
-    return r;
-}
-
 __device__ __forceinline__ uint32_t find_frame(const uint32_t* offsets, uint32_t n_frames, uint32_t item) {
     uint32_t lo = 0, hi = n_frames;  // offsets[lo] <= item < offsets[hi]
     while (hi - lo > 1) {
@@ -546,19 +497,30 @@ __device__ __forceinline__ uint32_t find_frame(const uint32_t* offsets, uint32_t
     return lo;
 }
 
-// Warp-wide inclusive scan of 6 int64 lanes (wrapping adds).
-__device__ __forceinline__ Moment warp_inclusive_scan_moment(Moment v) {
-    const int lane = threadIdx.x & 31;
-    long long x[6] = {v.Mx, v.My, v.Mxx, v.Myy, v.Mxy, v.W};
+// Inclusive scan of 6 int64 moment lanes within groups of WIDTH lanes
+// (32: the whole warp).  W, Mx and My are scanned in 32 bits: over at most
+// 128 points their sums stay below 2^31 (W <= 361, rx, ry < 2^15), so the
+// result equals the int64 (wrapping) sums.  Callers keep every partial sum
+// within 128 points.
+template <int WIDTH>
+__device__ __forceinline__ Moment scan_moment(const Moment& v) {
+    const int pos = (threadIdx.x & 31) & (WIDTH - 1);
+    uint32_t mx = (uint32_t)v.Mx, my = (uint32_t)v.My, mw = (uint32_t)v.W;
+    long long xx = v.Mxx, yy = v.Myy, xy = v.Mxy;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-#pragma unroll
-        for (int j = 0; j < 6; j++) {
-            const long long y = shfl_up_ll(x[j], o);
-            if (lane >= o) x[j] = wadd(x[j], y);
+    for (int o = 1; o < WIDTH; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, mx, o, WIDTH);
+        const uint32_t b = __shfl_up_sync(0xffffffffu, my, o, WIDTH);
+        const uint32_t c = __shfl_up_sync(0xffffffffu, mw, o, WIDTH);
+        const long long d = (long long)__shfl_up_sync(0xffffffffu, (unsigned long long)xx, o, WIDTH);
+        const long long e = (long long)__shfl_up_sync(0xffffffffu, (unsigned long long)yy, o, WIDTH);
+        const long long f = (long long)__shfl_up_sync(0xffffffffu, (unsigned long long)xy, o, WIDTH);
+        if (pos >= o) {
+            mx += a; my += b; mw += c;
+            xx = wadd(xx, d); yy = wadd(yy, e); xy = wadd(xy, f);
         }
     }
-    return Moment{x[0], x[1], x[2], x[3], x[4], x[5]};
+    return Moment{(long long)mx, (long long)my, xx, yy, xy, (long long)mw};
 }
 __device__ __forceinline__ Moment warp_sum_moment(Moment v) {
     long long x[6] = {v.Mx, v.My, v.Mxx, v.Myy, v.Mxy, v.W};
@@ -583,7 +545,8 @@ __device__ __forceinline__ void cluster_sort(const FrameSet& fs, const uint32_t*
     __shared__ long long red_m[32][6];
     __shared__ uint32_t red32[33];
     __shared__ uint32_t s_item, s_flag;
-    uint32_t* hist = reinterpret_cast<uint32_t*>(smem_keys + sort_cap);  // radix counters (global-memory sorts)
+    // radix counters of the global-memory sorts, after the padded key array
+    uint32_t* hist = reinterpret_cast<uint32_t*>(smem_keys + kpad_size(sort_cap));
     const uint32_t total = work_offsets[n_frames];
     for (;;) {
         __syncthreads();
@@ -599,83 +562,101 @@ __device__ __forceinline__ void cluster_sort(const FrameSet& fs, const uint32_t*
         const uint32_t n = ext.count, start = ext.start;
         // sort by (theta, packed point): the reference's (cluster, slope)
         // order (main.cpp:737-750) with ties fixed by the point.  Up to
-        // sort_cap keys: a bitonic sort in registers sized to the cluster;
-        // larger clusters (4K frames only): radix sort in global memory.
+        // sort_cap keys sort in shared memory (padded layout, key i at
+        // kpad(i)): a register bitonic network for up to 4 keys per thread,
+        // a merge sort above; larger clusters (4K frames only) radix-sort
+        // in global memory (plain layout).
         unsigned long long* X = smem_keys;
         const unsigned long long* src = F.sortbuf + start;
+        uint32_t pad_mask = ~0u;
         if (n <= sort_cap) {
             if (LARGE) {
-                if (n <= THREADS * 8) sort_keys_regs<THREADS, 8>(src, n, X);
-                else if (n <= THREADS * 16) sort_keys_regs<THREADS, 16>(src, n, X);
-                else sort_keys_regs<THREADS, 32>(src, n, X);
+                if (n <= THREADS * 8) merge_sort_keys<THREADS, 8>(src, n, X);
+                else if (n <= THREADS * 16) merge_sort_keys<THREADS, 16>(src, n, X);
+                else merge_sort_keys<THREADS, 32>(src, n, X);
             } else {
                 if (n <= THREADS * 2) sort_keys_regs<THREADS, 2>(src, n, X);
                 else if (n <= THREADS * 4) sort_keys_regs<THREADS, 4>(src, n, X);
-                else if (n <= THREADS * 8) sort_keys_regs<THREADS, 8>(src, n, X);
-                else sort_keys_regs<THREADS, 16>(src, n, X);
+                else if (n <= THREADS * 8) merge_sort_keys<THREADS, 8>(src, n, X);
+                else merge_sort_keys<THREADS, 16>(src, n, X);
             }
         } else {
             X = block_radix_sort_u64<THREADS>(F.sortbuf + start,
                                               reinterpret_cast<unsigned long long*>(F.errbuf + 2ull * start), n,
                                               hist, red32, &s_flag);
+            pad_mask = 0u;
             __syncthreads();
         }
+        auto at = [&](uint32_t i) -> unsigned long long& { return X[i + ((i >> 4) & pad_mask)]; };
+        // The rest runs per warp over contiguous ranges of 128-point chunks
+        // (32 lanes x SEG consecutive points).
+        constexpr uint32_t W = THREADS / 32, SEG = 4, CH = 32 * SEG;
+        const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const uint32_t nch = (n + CH - 1) / CH, ch0 = nch * w / W, ch1 = nch * (w + 1) / W;
+        const uint32_t r0 = ch0 * CH, r1 = min(n, ch1 * CH);
         // ClusterPoints out; the key slot is reused for the line-fit inputs
-        // (four points per thread in flight, so their image reads overlap)
-        for (uint32_t i0 = threadIdx.x; i0 < n; i0 += 4 * blockDim.x) {
+        // (four rows in flight, so their image reads overlap), and the
+        // warp's moment total for the scan below
+        Moment t{0, 0, 0, 0, 0, 0};
+        for (uint32_t i0 = r0 + lane; i0 < r1; i0 += 4 * 32) {
             unsigned long long k[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const uint32_t i = i0 + u * blockDim.x;
-                k[u] = i < n ? X[i] : 0ull;
+                const uint32_t i = i0 + u * 32;
+                k[u] = i < r1 ? at(i) : 0ull;
             }
             unsigned long long v[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) v[u] = linefit_rxyw((uint32_t)k[u], F.width, F.height, F.grey);
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const uint32_t i = i0 + u * blockDim.x;
-                if (i < n) {
+                const uint32_t i = i0 + u * 32;
+                if (i < r1) {
                     const uint32_t packed = (uint32_t)k[u];
                     atag_cluster_point cp;
                     cp.packed_x = (uint16_t)packed;
                     cp.packed_y = (uint16_t)(packed >> 16);
                     cp.slope = float_from_order_key((uint32_t)(k[u] >> 32));
                     F.cluster_points[start + i] = cp;
-                    X[i] = v[u];
+                    at(i) = v[u];
+                    t = m_add(t, moment_of(v[u]));
                 }
             }
         }
+        // segmented inclusive scan of the moments (main.cpp:796-801).  The
+        // carry into a warp's range is the sum of the earlier warps' totals;
+        // per chunk, lane l first sums its SEG points (4l .. 4l + 3), one
+        // warp scan of those 32 sums gives each segment's offset, then rows
+        // of 32 consecutive points add a scan within their segment to its
+        // offset, so consecutive lanes store consecutive LineFitPoints.
+        t = warp_sum_moment(t);
+        if (lane == 0) {
+            red_m[w][0] = t.Mx; red_m[w][1] = t.My; red_m[w][2] = t.Mxx;
+            red_m[w][3] = t.Myy; red_m[w][4] = t.Mxy; red_m[w][5] = t.W;
+        }
         __syncthreads();
-        // segmented inclusive scan of the moments (main.cpp:796-801): warp w
-        // owns a contiguous range of 32-point chunks; warp totals first, then
-        // chunk by chunk a warp scan plus the running carry, so consecutive
-        // lanes store consecutive LineFitPoints
-        {
-            constexpr uint32_t W = THREADS / 32;
-            const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-            const uint32_t nch = (n + 31) / 32, ch0 = nch * w / W, ch1 = nch * (w + 1) / W;
-            Moment t{0, 0, 0, 0, 0, 0};
-            for (uint32_t c = ch0; c < ch1; c++) {
-                const uint32_t i = c * 32 + lane;
-                if (i < n) t = m_add(t, moment_of(X[i]));
+        Moment carry{0, 0, 0, 0, 0, 0};
+        for (uint32_t k = 0; k < w; k++)
+            carry = m_add(carry, Moment{red_m[k][0], red_m[k][1], red_m[k][2], red_m[k][3], red_m[k][4],
+                                        red_m[k][5]});
+        for (uint32_t c = ch0; c < ch1; c++) {
+            const uint32_t c0 = c * CH;
+            Moment seg{0, 0, 0, 0, 0, 0};
+#pragma unroll
+            for (uint32_t q = 0; q < SEG; q++) {
+                const uint32_t i = c0 + lane * SEG + q;
+                if (i < n) seg = m_add(seg, moment_of(at(i)));
             }
-            t = warp_sum_moment(t);
-            if (lane == 0) {
-                red_m[w][0] = t.Mx; red_m[w][1] = t.My; red_m[w][2] = t.Mxx;
-                red_m[w][3] = t.Myy; red_m[w][4] = t.Mxy; red_m[w][5] = t.W;
-            }
-            __syncthreads();
-            Moment carry{0, 0, 0, 0, 0, 0};
-            for (uint32_t k = 0; k < w; k++)
-                carry = m_add(carry, Moment{red_m[k][0], red_m[k][1], red_m[k][2], red_m[k][3], red_m[k][4],
-                                            red_m[k][5]});
-            for (uint32_t c = ch0; c < ch1; c++) {
-                const uint32_t i = c * 32 + lane;
-                const Moment v = i < n ? moment_of(X[i]) : Moment{0, 0, 0, 0, 0, 0};
-                const Moment incl = warp_inclusive_scan_moment(v);
-                if (i < n) store_moment(F.line_fit + start + i, m_add(carry, incl));
-                carry = m_add(carry, shfl_moment(incl, 31));
+            const Moment incl = scan_moment<32>(seg);
+            const Moment off = m_add(carry, m_sub(incl, seg));
+            carry = m_add(carry, shfl_moment(incl, 31));
+#pragma unroll
+            for (uint32_t r = 0; r < SEG; r++) {
+                const uint32_t i = c0 + r * 32 + lane;
+                const Moment m = i < n ? moment_of(at(i)) : Moment{0, 0, 0, 0, 0, 0};
+                const Moment in_seg = scan_moment<SEG>(m);
+                const Moment base = shfl_moment(off, (int)(r * (32 / SEG) + lane / SEG));
+                if (i < n) store_moment(F.line_fit + start + i, m_add(base, in_seg));
             }
         }
         __syncthreads();
