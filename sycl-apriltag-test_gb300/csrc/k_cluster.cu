@@ -177,10 +177,9 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     __syncthreads();
 
     // A: enumerate points in the reference's test order (R, BL unless it
-    // would duplicate, B, BR: find_boundaries.cpp:128-150).  First a 4-bit
-    // emission mask per pixel, then positions from one block scan, then the
-    // pair key of each emitted point goes into the CTA table and the point
-    // into the staging list.
+    // would duplicate, B, BR: find_boundaries.cpp:128-150): a 4-bit
+    // emission mask per pixel, positions from one block scan, and each
+    // point (pixel and test) into the staging list.
     const int lane = threadIdx.x & 31;
     const int r = threadIdx.x / (BP_W / 4), cbase = (threadIdx.x % (BP_W / 4)) * 4;
     const int y = y0 + r;
@@ -200,62 +199,60 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         masks |= m << (4 * k);
     }
     uint32_t nst;
-    uint32_t pos = block_exclusive_scan_u32((uint32_t)__popc(masks), red, &nst);
-    if (masks) {
-        unsigned long long last_key = EMPTY_KEY;
-        int last_ls = -1;
+    const uint32_t pos0 = block_exclusive_scan_u32((uint32_t)__popc(masks), red, &nst);
+    {
+        uint32_t pos = pos0;
         for (uint32_t mm = masks; mm; mm &= mm - 1) {
-            const int bit = __ffs(mm) - 1, k = bit >> 2, t = bit & 3;
-            const int xo = cbase + k, x = x0 + xo, c = xo + 1;
-            const int rr = r + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
-            const uint32_t p = lab[r][c], q = lab[rr][cc];
-            const uint32_t lp = p & BP_VALUE, lq = q & BP_VALUE;
-            const int dir = (q & LABEL_PIXEL_MASK) > (p & LABEL_PIXEL_MASK) ? 1 : 0;
-            const unsigned long long key = ((unsigned long long)min(lp, lq) << 32) | max(lp, lq);
-            int ls;
-            if (key == last_key) {  // consecutive points of a thread mostly share their pair
-                ls = last_ls;
-            } else {
-                ls = local_insert(T, key);
-                last_key = key;
-                last_ls = ls;
-            }
-            uint32_t e = stage_entry(ls < 0 ? 0 : ls, xo, r, t, dir);
-            if (ls < 0) {  // CTA table full: account for and list the point directly
-                e |= STAGE_DIRECT;
-                const uint32_t gs = global_insert(F, key);
-                const uint32_t xd = 2u * (uint32_t)x + 1u, yd = 2u * (uint32_t)y;
-                const int gx = dir ? 1 : -1;
-                if (gs == INVALID) {
-                    atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
-                } else {
-                    global_flush(F, gs, 1, xd, xd, yd, yd, gx, 0, (unsigned long long)(long long)((int)xd * gx));
-                    const uint32_t at = atomicAdd(F.counters + CNT_POINTS, 1u);
-                    if (at < F.point_cap) F.points[at] = ((unsigned long long)gs << 32) | stage_packed(e, x0, y0);
-                    else atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
-                }
-            }
-            stage[pos++] = e;
+            const int bit = __ffs(mm) - 1;
+            stage[pos++] = stage_entry(0, cbase + (bit >> 2), r, bit & 3, 0);
         }
     }
-    __syncthreads();
-
-    // B: per-pair sums of the staged points (warp groups by table slot)
-    for (uint32_t b0 = (threadIdx.x & ~31u); b0 < nst; b0 += blockDim.x) {
-        const uint32_t i = b0 + lane;
-        const uint32_t e0 = i < nst ? stage[i] : STAGE_DIRECT;
-        const bool v = !(e0 & STAGE_DIRECT);
-        const uint32_t e = v ? e0 : 0u;
-        const uint32_t ls = v ? ((e >> 13) & 255) : 0xFFFFu;
-        const uint32_t xd = 2u * (uint32_t)(x0 + (e & 63)) + 1u, yd = 2u * (uint32_t)(y0 + ((e >> 6) & 15));
-        const int gx = ((e >> 12) & 1) ? 1 : -1;
-        const unsigned m = __match_any_sync(0xffffffffu, ls);
-        const uint32_t cnt = __reduce_add_sync(m, v ? 1u : 0u);
+    __syncwarp();
+    // Then the warp takes its points 32 at a time: pair key, CTA table slot
+    // (one insert per distinct key of the round) and the per-pair sums of
+    // the round's points, merged into the table by one lane per key.
+    const uint32_t wbeg = __shfl_sync(0xFFFFFFFFu, pos0, 0);
+    const uint32_t wend = __shfl_sync(0xFFFFFFFFu, pos0 + (uint32_t)__popc(masks), 31);
+    for (uint32_t b0 = wbeg; b0 < wend; b0 += 32) {
+        const uint32_t i = b0 + (uint32_t)lane;
+        const bool v = i < wend;
+        uint32_t e = v ? stage[i] : 0u;
+        const int xo = (int)(e & 63), ro = (int)((e >> 6) & 15), t = (int)((e >> 10) & 3), c = xo + 1;
+        const int rr = ro + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
+        const uint32_t p = lab[ro][c], q = lab[rr][cc];
+        const uint32_t lp = p & BP_VALUE, lq = q & BP_VALUE;
+        const int dir = (q & LABEL_PIXEL_MASK) > (p & LABEL_PIXEL_MASK) ? 1 : 0;
+        const unsigned long long key = v ? (((unsigned long long)min(lp, lq) << 32) | max(lp, lq)) : EMPTY_KEY;
+        const unsigned m = __match_any_sync(0xFFFFFFFFu, key);
+        const int leader = __ffs(m) - 1;
+        int ls = 0;
+        if (v && lane == leader) ls = local_insert(T, key);
+        ls = __shfl_sync(0xFFFFFFFFu, ls, leader);
+        const uint32_t xd = 2u * (uint32_t)(x0 + xo) + 1u, yd = 2u * (uint32_t)(y0 + ro);
+        const int gx = dir ? 1 : -1;
+        e |= (uint32_t)dir << 12;
+        if (v && ls < 0) {  // CTA table full: account for and list the point directly
+            e |= STAGE_DIRECT;
+            const uint32_t gs = global_insert(F, key);
+            if (gs == INVALID) {
+                atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
+            } else {
+                global_flush(F, gs, 1, xd, xd, yd, yd, gx, 0, (unsigned long long)(long long)((int)xd * gx));
+                const uint32_t at = atomicAdd(F.counters + CNT_POINTS, 1u);
+                if (at < F.point_cap) F.points[at] = ((unsigned long long)gs << 32) | stage_packed(e, x0, y0);
+                else atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
+            }
+        } else {
+            e |= (uint32_t)ls << 13;
+        }
+        if (v) stage[i] = e;
+        const bool a = v && ls >= 0;
+        const uint32_t cnt = __reduce_add_sync(m, a ? 1u : 0u);
         const uint32_t xmn = __reduce_min_sync(m, xd), xmx = __reduce_max_sync(m, xd);
         const uint32_t ymn = __reduce_min_sync(m, yd), ymx = __reduce_max_sync(m, yd);
-        const int sgx = __reduce_add_sync(m, v ? gx : 0);
-        const int spx = __reduce_add_sync(m, v ? (int)xd * gx : 0);
-        if (v && lane == __ffs(m) - 1) {
+        const int sgx = __reduce_add_sync(m, a ? gx : 0);
+        const int spx = __reduce_add_sync(m, a ? (int)xd * gx : 0);
+        if (a && lane == leader) {
             atomicAdd(&T.cnt[ls], cnt);
             atomicMin(&T.xmin[ls], xmn);
             atomicMax(&T.xmax[ls], xmx);
