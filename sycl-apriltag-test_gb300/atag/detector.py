@@ -29,7 +29,7 @@ class Detector:
     """
 
     def __init__(self, max_width: int, max_height: int, max_frames: int = 1, max_total_pixels: int = 0,
-                 config=None, quad_capacity: int = 1024):
+                 config=None, quad_capacity: int = 1024, keep_intermediates: bool = False):
         self.L = lib.init()
         self.cfg = config or lib.default_config()
         self.max_frames = max_frames
@@ -47,6 +47,14 @@ class Detector:
         self.d_stats = torch.zeros(max_frames * FRAME_STATS.itemsize, dtype=torch.uint8, device="cuda")
         self._frames = []
         self._n = 0
+        self.keep_intermediates(keep_intermediates)
+
+    def keep_intermediates(self, keep: bool = True):
+        """With keep, later calls also write the reference's full scratch and
+        sizes arrays (zeros away from component roots), which `views` shows;
+        by default only what the later stages read is written."""
+        lib.check(self.L.atag_detector_keep_intermediates(self.handle, 1 if keep else 0),
+                  "atag_detector_keep_intermediates")
 
     def close(self):
         if self.handle:
@@ -160,7 +168,10 @@ class Detector:
         raise ValueError("pointer outside the workspace")
 
     def views(self, i: int = 0) -> dict:
-        """Copies frame i's intermediates to the host (numpy records)."""
+        """Copies frame i's intermediates to the host (numpy records).
+        `sizes` is exact at component roots (the labels' values); elsewhere it
+        holds the reference's zeros only on a detector that keeps
+        intermediates."""
         v = FrameViews()
         lib.check(self.L.atag_detector_views(self.handle, i, ctypes.byref(v)), "atag_detector_views")
         st = self.stats()[i]

@@ -46,6 +46,7 @@ _SIGNATURES = {
     "atag_detect": (_ST, [_P, _P, _SZ, _SZ, _P, _SZ, _P, _P]),
     "atag_detect_host": (_ST, [_P, _P, _SZ, _SZ, _P, _SZ, _P, _P]),
     "atag_detector_views": (_ST, [_P, _SZ, ctypes.POINTER(FrameViews)]),
+    "atag_detector_keep_intermediates": (_ST, [_P, ctypes.c_int]),
     "atag_detector_set_stage_events": (_ST, [_P, ctypes.POINTER(_P), _SZ]),
     "atag_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
     "atag_detector_get_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),

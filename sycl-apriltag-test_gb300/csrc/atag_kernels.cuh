@@ -64,6 +64,11 @@ struct FrameDesc {
     uint32_t quad_cap;
     atag_frame_stats* stats;
     uint32_t* counters;                // per-frame work counters (see Counter)
+    // 1: write the reference's complete segmentation arrays (every parent
+    // compressed to its root, block information words at odd rows, zero
+    // sizes away from roots).  0 (fused batches): only what later stages
+    // read, i.e. parents at even rows and sizes at the roots.
+    uint32_t stage_outputs;
 };
 
 // The frames a launch works on: a device table (batches) or one descriptor

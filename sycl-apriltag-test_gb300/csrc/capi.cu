@@ -241,6 +241,7 @@ struct atag_detector {
     std::vector<FrameDesc> cur;      // table of the last call
     std::vector<cudaEvent_t> stage_events;
     atag_tuning tuning{16, 16, (int32_t)CF_SMALL_CAP, 8, 2, 8, 2};
+    bool keep_intermediates = false;
 };
 
 namespace {
@@ -401,6 +402,7 @@ atag_status atag_image_segmentation(const uint8_t* thr, uint32_t* scratch, uint3
     FrameDesc d = blank();
     d.width = (uint32_t)w; d.height = (uint32_t)h; d.factor = 1;
     d.thr = const_cast<uint8_t*>(thr); d.scratch = scratch; d.labels = labels; d.sizes = sizes;
+    d.stage_outputs = 1;
     return launch_segmentation(single(d), w, h, 1, (cudaStream_t)stream);
 }
 
@@ -748,6 +750,7 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
         d.quads = d_quads + i * quad_cap;
         d.quad_cap = (uint32_t)quad_cap;
         d.stats = d_stats + i;
+        d.stage_outputs = det->keep_intermediates ? 1u : 0u;
     }
     const FrameDesc* d_table;
     atag_status st = upload_table(det, t, s, &d_table);
@@ -852,6 +855,12 @@ atag_status atag_detector_set_stage_events(atag_detector* det, void* const* even
     if (n != ATAG_STAGE_COUNT + 1)
         return fail(ATAG_ERR_INVALID_ARGUMENT, "set_stage_events: need %d events, got %zu", ATAG_STAGE_COUNT + 1, n);
     for (size_t i = 0; i < n; i++) det->stage_events.push_back((cudaEvent_t)events[i]);
+    return ATAG_OK;
+}
+
+atag_status atag_detector_keep_intermediates(atag_detector* det, int keep) {
+    if (!det) return fail(ATAG_ERR_INVALID_ARGUMENT, "keep_intermediates: null detector");
+    det->keep_intermediates = keep != 0;
     return ATAG_OK;
 }
 

@@ -312,9 +312,11 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         *reinterpret_cast<uint2*>(F.scratch + id) = parents;
         uint2 sz = make_uint2(rw == 2 * l ? cnt[2 * l] : 0u, rb == 2 * l + 1 ? cnt[2 * l + 1] : 0u);
         *reinterpret_cast<uint2*>(F.sizes + id) = sz;
-        *reinterpret_cast<uint2*>(F.sizes + id + w) = make_uint2(0u, 0u);
-        // the reference keeps the block's information word at scratch[id + w]
-        *reinterpret_cast<uint2*>(F.scratch + id + w) = make_uint2(L.info, 0u);
+        if (F.stage_outputs) {
+            *reinterpret_cast<uint2*>(F.sizes + id + w) = make_uint2(0u, 0u);
+            // the reference keeps the block's information word at scratch[id + w]
+            *reinterpret_cast<uint2*>(F.scratch + id + w) = make_uint2(L.info, 0u);
+        }
     }
 }
 
@@ -414,7 +416,7 @@ __global__ void __launch_bounds__(256) k_ccl_final(const __grid_constant__ Frame
         if (capped && F.counters) atomicOr(F.counters + CNT_STATUS, ATAG_DEVFLAG_UF_ITERATION_CAP);
         // every slot ends pointing at its root, as the reference's scratch
         // does after its last compression (segmentation.cpp:309)
-        *reinterpret_cast<uint4*>(F.scratch + id) = make_uint4(r[0], r[1], r[2], r[3]);
+        if (F.stage_outputs) *reinterpret_cast<uint4*>(F.scratch + id) = make_uint4(r[0], r[1], r[2], r[3]);
         // fold the tile counts of non-root slots into their roots; a root's
         // own entry is left alone (other threads add to it)
         const uint32_t sz[4] = {s4.x, s4.y, s4.z, s4.w};
@@ -425,7 +427,8 @@ __global__ void __launch_bounds__(256) k_ccl_final(const __grid_constant__ Frame
             if (r[k] == sid) any_root = true;
             else if (sz[k]) atomicAdd(F.sizes + r[k], sz[k]);
         }
-        if (!any_root) {
+        if (!F.stage_outputs) {
+        } else if (!any_root) {
             *reinterpret_cast<uint4*>(F.sizes + id) = make_uint4(0u, 0u, 0u, 0u);
         } else {
 #pragma unroll

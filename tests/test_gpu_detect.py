@@ -23,7 +23,7 @@ def _run(det, img):
 @pytest.fixture(scope="module")
 def det1080():
     from atag.detector import Detector
-    return Detector(1920, 1080)
+    return Detector(1920, 1080, keep_intermediates=True)
 
 
 @pytest.mark.parametrize("name", ["decimate", "decimate4", "decimate2"])
@@ -50,11 +50,28 @@ def test_detect_small_and_edge_frames(det1080):
         assert_detect_matches(views, quads, res)
 
 
+def test_default_detector_skips_only_unread_intermediates(det1080):
+    """A detector that does not keep intermediates gives the same quads,
+    labels and component sizes (at every label's root) as one that writes
+    the reference's full segmentation arrays."""
+    from atag.detector import Detector
+    lean = Detector(1920, 1080)
+    for seed in (5, 6):
+        img = synth_frame("1080p", seed)
+        q_full, v_full = _run(det1080, img)
+        q_lean, v_lean = _run(lean, img)
+        assert len(q_full) > 0 and q_full.tobytes() == q_lean.tobytes()
+        assert np.array_equal(v_full["labels"], v_lean["labels"])
+        roots = np.unique(v_full["labels"].ravel() & 0x7FFFFFFF)
+        assert np.array_equal(v_full["sizes"][roots], v_lean["sizes"][roots])
+        assert np.array_equal(v_full["line_fit"], v_lean["line_fit"])
+
+
 def test_detect_decimate2():
     from atag import lib
     from atag.detector import Detector
     cfg = lib.default_config(decimate=2)
-    det = Detector(960, 540, config=cfg)
+    det = Detector(960, 540, config=cfg, keep_intermediates=True)
     img = synth_frame("1080p", 3)
     quads, views = _run(det, img)
     res = oracle.detect(img, oracle.default_config(decimate=2))
@@ -65,7 +82,7 @@ def test_detect_decimate2():
 def test_detect_aligned_peak_index_mode(ref_images):
     from atag import lib
     from atag.detector import Detector
-    det = Detector(1920, 1080, config=lib.default_config(compat_peak_index=0))
+    det = Detector(1920, 1080, config=lib.default_config(compat_peak_index=0), keep_intermediates=True)
     for name in ("decimate", "decimate2"):
         img = ref_images[name]
         quads, views = _run(det, img)
@@ -111,7 +128,7 @@ def test_detect_4k_stress():
     radix path) and deep union-find merges."""
     from atag.detector import Detector
     img = synth_frame("4k", 1)
-    det = Detector(3840, 2160)
+    det = Detector(3840, 2160, keep_intermediates=True)
     quads, views = _run(det, img)
     res = oracle.detect(img)
     assert_detect_matches(views, quads, res)

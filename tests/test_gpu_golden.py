@@ -35,7 +35,7 @@ def golden():
 @pytest.fixture(scope="module")
 def det():
     from atag.detector import Detector
-    return Detector(1920, 1080)
+    return Detector(1920, 1080, keep_intermediates=True)
 
 
 def _check(golden_entry, stage, arr):
