@@ -226,6 +226,7 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __shared__ uint8_t pix[PH][PW];  // rows y0-1.., cols x0-1..
     __shared__ uint32_t par[2 * CCL_THREADS];
     __shared__ uint32_t cnt[2 * CCL_THREADS];
+    __shared__ uint32_t row_runs[CCL_BY][2];  // S-link ballots of each tile row (255, 0 forest)
 
     // the tile's pixels plus a one-pixel halo (x0 - 1 .. x0 + 2 CCL_BX, y0 - 1
     // ..), loaded as aligned 32-bit words (x0 and w are multiples of 4)
@@ -262,37 +263,49 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     const uint32_t lane = (uint32_t)tx;
     const unsigned sw = __ballot_sync(0xFFFFFFFFu, live && tx > 0 && (L.wmask & 8u));
     const unsigned sb = __ballot_sync(0xFFFFFFFFu, live && tx > 0 && (L.bmask & 8u));
-    {
-        const unsigned le = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
-        const uint32_t row0 = (uint32_t)ty * CCL_BX;
-        par[2 * l] = 2 * (row0 + 31 - __clz(~sw & le));
-        par[2 * l + 1] = 2 * (row0 + 31 - __clz(~sb & le)) + 1;
+    const unsigned le = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+    const uint32_t hw = 31 - __clz(~sw & le), hb = 31 - __clz(~sb & le);  // run heads (lanes)
+    const uint32_t row0 = (uint32_t)ty * CCL_BX;
+    par[2 * l] = 2 * (row0 + hw);
+    par[2 * l + 1] = 2 * (row0 + hb) + 1;
+    if (lane == 0) {
+        row_runs[ty][0] = sw;
+        row_runs[ty][1] = sb;
     }
     __syncthreads();
-    // P, Q, R links (up-left, up, up-right) inside the tile.  Within a run,
-    // the block above-left of lane i is the block above lane i - 1: the P
-    // link of i is left out when i - 1 is in the same run and has its Q
-    // link (the same union), and likewise R against i + 1
+    // P, Q, R links (up-left, up, up-right) inside the tile.  Every block
+    // of a run shares the run's set, so a run needs one union per run of
+    // the row above that any of its blocks links to: the run's last lane
+    // ORs the above-row blocks its lanes link to (segmented scan), keeps the
+    // first linked block of each above run and makes those unions.
     if (ty > 0) {
-        const unsigned qw = __ballot_sync(0xFFFFFFFFu, live && (L.wmask & 2u));
-        const unsigned qb = __ballot_sync(0xFFFFFFFFu, live && (L.bmask & 2u));
+        uint32_t aw = 0, ab = 0;
         if (live) {
-            const uint32_t up = l - CCL_BX;
-            const bool skip_pw = ((sw >> lane) & 1u) && ((qw >> (lane - 1)) & 1u);
-            const bool skip_pb = ((sb >> lane) & 1u) && ((qb >> (lane - 1)) & 1u);
-            const bool skip_rw = lane < 31 && ((sw >> (lane + 1)) & 1u) && ((qw >> (lane + 1)) & 1u);
-            const bool skip_rb = lane < 31 && ((sb >> (lane + 1)) & 1u) && ((qb >> (lane + 1)) & 1u);
-            if (L.wmask & 2u) uf_union((volatile uint32_t*)par, 2 * l, 2 * up);
-            if (L.bmask & 2u) uf_union((volatile uint32_t*)par, 2 * l + 1, 2 * up + 1);
+            const uint32_t me = 1u << lane;
+            if (L.wmask & 2u) aw |= me;
+            if (L.bmask & 2u) ab |= me;
             if (tx > 0) {
-                if ((L.wmask & 1u) && !skip_pw) uf_union((volatile uint32_t*)par, 2 * l, 2 * (up - 1));
-                if ((L.bmask & 1u) && !skip_pb) uf_union((volatile uint32_t*)par, 2 * l + 1, 2 * (up - 1) + 1);
+                if (L.wmask & 1u) aw |= me >> 1;
+                if (L.bmask & 1u) ab |= me >> 1;
             }
             if (tx < CCL_BX - 1) {
-                if ((L.wmask & 4u) && !skip_rw) uf_union((volatile uint32_t*)par, 2 * l, 2 * (up + 1));
-                if ((L.bmask & 4u) && !skip_rb) uf_union((volatile uint32_t*)par, 2 * l + 1, 2 * (up + 1) + 1);
+                if (L.wmask & 4u) aw |= me << 1;
+                if (L.bmask & 4u) ab |= me << 1;
             }
         }
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, aw, o), yb = __shfl_up_sync(0xFFFFFFFFu, ab, o);
+            if (lane >= hw + o) aw |= yw;
+            if (lane >= hb + o) ab |= yb;
+        }
+        const bool last_w = lane == 31 || !((sw >> (lane + 1)) & 1u);
+        const bool last_b = lane == 31 || !((sb >> (lane + 1)) & 1u);
+        const uint32_t up0 = row0 - CCL_BX;
+        uint32_t ew = last_w ? (aw & ~((aw << 1) & row_runs[ty - 1][0])) : 0u;
+        uint32_t eb = last_b ? (ab & ~((ab << 1) & row_runs[ty - 1][1])) : 0u;
+        for (; ew; ew &= ew - 1) uf_union((volatile uint32_t*)par, 2 * (row0 + hw), 2 * (up0 + __ffs(ew) - 1));
+        for (; eb; eb &= eb - 1) uf_union((volatile uint32_t*)par, 2 * (row0 + hb) + 1, 2 * (up0 + __ffs(eb) - 1) + 1);
     }
     __syncthreads();
     uint32_t rw = find_root_volatile((volatile uint32_t*)par, 2 * l);
