@@ -388,7 +388,7 @@ atag_status atag_refine_backward(const float *d_image, size_t width, size_t heig
  * defaults below; the autotuner (sycl-apriltag-test_gb300/atag/autotune.py)
  * picks them per GPU and workload. */
 typedef struct atag_tuning {
-    int32_t ccl_tile_rows;        /* 8 or 16 rows of 2x2 blocks per CCL tile (16)   */
+    int32_t ccl_tile_rows;        /* 8, 16 or 32 rows of 2x2 blocks per CCL tile (16) */
     int32_t boundary_tile_rows;   /* 8 or 16 pixel rows per boundary tile (16)      */
     int32_t small_cluster_max;    /* clusters up to this size use the 128-thread
                                      kernel, larger ones the 512-thread one

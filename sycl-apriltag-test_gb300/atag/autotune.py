@@ -3,18 +3,18 @@
 Coordinate descent over a small space of tile and block shapes: starting
 from the current shapes, each parameter in turn is set to every candidate
 value with the others fixed, the detector is timed on the caller's frames
-(CUDA events, median of `reps` runs after one warm-up) and the fastest value
-is kept; the sweep repeats until nothing changes or `passes` run out.
+(one detect call captured as a CUDA graph, `reps` replays between CUDA
+events after a warm-up) and the fastest value is kept; the sweep repeats
+until nothing changes or `passes` run out.
 Every shape gives bit-identical results, so tuning only changes speed.
 Results are cached in a JSON file keyed by GPU, SM count, decimation and
 the batch's frame sizes.
 """
 import json
 import os
-import statistics
 
 SPACE = {
-    "ccl_tile_rows": [8, 16],
+    "ccl_tile_rows": [8, 16, 32],
     "boundary_tile_rows": [8, 16],
     "small_cluster_max": [512, 1024, 2048],
     "small_ctas_per_sm": [4, 8, 12],
@@ -55,6 +55,9 @@ def workload_key(det, frames):
 
 
 def measure_fn(det, frames, reps=5):
+    """Milliseconds per detect call of `det` on `frames` under a tuning: the
+    call is captured as a CUDA graph and replayed `reps` times back to back,
+    the way a batched caller runs it."""
     import torch
     stream = torch.cuda.Stream()
 
@@ -62,15 +65,20 @@ def measure_fn(det, frames, reps=5):
         det.set_tuning(**tuning)
         with torch.cuda.stream(stream):
             det.enqueue(frames, stream=stream)  # warm-up
-            times = []
+        stream.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            det.enqueue(frames, stream=stream)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            graph.replay()
+            a.record(stream)
             for _ in range(reps):
-                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                a.record(stream)
-                det.enqueue(frames, stream=stream)
-                b.record(stream)
-                b.synchronize()
-                times.append(a.elapsed_time(b))
-        return statistics.median(times)
+                graph.replay()
+            b.record(stream)
+        b.synchronize()
+        del graph
+        return a.elapsed_time(b) / reps
     return measure
 
 

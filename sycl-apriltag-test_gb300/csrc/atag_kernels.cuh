@@ -143,7 +143,9 @@ __global__ void k_threshold(const __grid_constant__ FrameSet fs, int min_diff, i
 __global__ void k_ccl_local_r8(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_local_r16(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_border_r8(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_local_r32(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_border_r16(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_border_r32(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_final(const __grid_constant__ FrameSet fs);
 __global__ void k_boundaries_dense(const __grid_constant__ FrameSet fs, uint32_t min_size);
 

@@ -628,7 +628,7 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
     };
 #define STAGE(i) do { atag_status m_ = mark(i); if (m_) return m_; } while (0)
     const atag_tuning& tu = det->tuning;
-    const int ccl_rows = tu.ccl_tile_rows == 8 ? 8 : 16;
+    const int ccl_rows = tu.ccl_tile_rows == 8 || tu.ccl_tile_rows == 32 ? tu.ccl_tile_rows : 16;
     const int bp_rows = tu.boundary_tile_rows == 8 ? 8 : 16;
     const size_t tiles_ccl = cdiv(mw / 2, 32) * cdiv(mh / 2, (size_t)ccl_rows);
     STAGE(0);
@@ -644,12 +644,14 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
     LAUNCHED();
     STAGE(3);
     if (ccl_rows == 8) k_ccl_local_r8<<<grid2(tiles_ccl, n), 32 * 8, 0, s>>>(fs);
+    else if (ccl_rows == 32) k_ccl_local_r32<<<grid2(tiles_ccl, n), 32 * 32, 0, s>>>(fs);
     else k_ccl_local_r16<<<grid2(tiles_ccl, n), 32 * 16, 0, s>>>(fs);
     LAUNCHED();
     STAGE(4);
     {
         const size_t border = tiles_ccl * (32 + 2 * (ccl_rows - 1));
         if (ccl_rows == 8) k_ccl_border_r8<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
+        else if (ccl_rows == 32) k_ccl_border_r32<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
         else k_ccl_border_r16<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
         LAUNCHED();
     }
@@ -872,8 +874,9 @@ atag_status atag_detector_get_tuning(const atag_detector* det, atag_tuning* out)
 
 atag_status atag_detector_set_tuning(atag_detector* det, const atag_tuning* t) {
     if (!det || !t) return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: null argument");
-    if ((t->ccl_tile_rows != 8 && t->ccl_tile_rows != 16) || (t->boundary_tile_rows != 8 && t->boundary_tile_rows != 16))
-        return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: tile rows must be 8 or 16");
+    if ((t->ccl_tile_rows != 8 && t->ccl_tile_rows != 16 && t->ccl_tile_rows != 32) ||
+        (t->boundary_tile_rows != 8 && t->boundary_tile_rows != 16))
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: CCL tile rows must be 8, 16 or 32, boundary tile rows 8 or 16");
     if (t->small_cluster_max < 1 || t->small_cluster_max > (int32_t)CF_SMALL_CAP)
         return fail(ATAG_ERR_INVALID_ARGUMENT, "set_tuning: small_cluster_max must be in [1, %u]", CF_SMALL_CAP);
     if (t->small_ctas_per_sm < 1 || t->small_ctas_per_sm > 16 || t->large_ctas_divisor < 1 ||

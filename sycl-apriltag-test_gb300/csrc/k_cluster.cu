@@ -148,24 +148,38 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     __shared__ uint32_t red[33];
     __shared__ uint32_t s_base;
 
-    // labels of the tile and its halo, then the size of each label's
-    // component: all label loads of a thread are issued before its size
-    // gathers, so the two dependent round trips overlap across iterations
+    // labels of the tile (16-byte loads of four) and its halo columns, then
+    // the size of each label's component: all label loads of a thread are
+    // issued before its size gathers
     {
-        constexpr int THREADS = BP_W / 4 * BP_H, NL = (BP_SH * BP_SW + THREADS - 1) / THREADS;
-        uint32_t lv[NL];
+        constexpr int THREADS = BP_W / 4 * BP_H, NQ = BP_SH * (BP_W / 4), NH = BP_SH * 2;
+        constexpr int NI = (NQ + NH + THREADS - 1) / THREADS;
+        uint4 lv[NI];
 #pragma unroll
-        for (int k = 0; k < NL; k++) {
-            const int i = threadIdx.x + k * THREADS, r = i / BP_SW, c = i % BP_SW;
-            const int y = y0 + r, x = x0 - 1 + c;
-            lv[k] = (i < BP_SH * BP_SW && x >= 0 && x < w && y < h) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
+        for (int k = 0; k < NI; k++) {
+            const int it = threadIdx.x + k * THREADS;
+            lv[k] = make_uint4(0u, 0u, 0u, 0u);
+            if (it < NQ) {
+                const int r = it / (BP_W / 4), y = y0 + r, x = x0 + 4 * (it % (BP_W / 4));
+                if (y < h && x < w) lv[k] = __ldg(reinterpret_cast<const uint4*>(F.labels + (size_t)y * w + x));
+            } else if (it < NQ + NH) {
+                const int hi = it - NQ, y = y0 + (hi >> 1), x = (hi & 1) ? x0 + BP_W : x0 - 1;
+                if (y < h && x >= 0 && x < w) lv[k].x = __ldg(F.labels + (size_t)y * w + x);
+            }
         }
 #pragma unroll
-        for (int k = 0; k < NL; k++) {
-            const int i = threadIdx.x + k * THREADS, r = i / BP_SW, c = i % BP_SW;
-            if (i < BP_SH * BP_SW) {
-                const bool big = __ldg(F.sizes + (lv[k] & LABEL_VALUE_MASK)) >= min_size;
-                lab[r][c] = lv[k] | (big ? BP_BIG : 0u);
+        for (int k = 0; k < NI; k++) {
+            const int it = threadIdx.x + k * THREADS;
+            auto tag = [&](uint32_t v) { return v | (__ldg(F.sizes + (v & LABEL_VALUE_MASK)) >= min_size ? BP_BIG : 0u); };
+            if (it < NQ) {
+                const int r = it / (BP_W / 4), c = 1 + 4 * (it % (BP_W / 4));
+                lab[r][c] = tag(lv[k].x);
+                lab[r][c + 1] = tag(lv[k].y);
+                lab[r][c + 2] = tag(lv[k].z);
+                lab[r][c + 3] = tag(lv[k].w);
+            } else if (it < NQ + NH) {
+                const int hi = it - NQ;
+                lab[hi >> 1][(hi & 1) ? BP_W + 1 : 0] = tag(lv[k].x);
             }
         }
     }

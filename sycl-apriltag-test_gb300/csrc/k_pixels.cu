@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(256) k_threshold(const __grid_constant__ Frame
 // (2) links that cross tile borders are merged in global memory;
 // (3) final labels, and tile counts folded into the component root.
 // ---------------------------------------------------------------------------
-constexpr int CCL_BX = 32;  // blocks per tile row; CCL_BY (8 or 16) rows is a tuning choice
+constexpr int CCL_BX = 32;  // blocks per tile row; CCL_BY (8, 16 or 32) rows is a tuning choice
 constexpr uint32_t UF_FIND_CAP = 1u << 23;   // longest parent chain followed
 constexpr uint32_t UF_UNION_CAP = 1u << 12;  // retries of one contended union
 
@@ -266,6 +266,8 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     const unsigned le = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
     const uint32_t hw = 31 - __clz(~sw & le), hb = 31 - __clz(~sb & le);  // run heads (lanes)
     const uint32_t row0 = (uint32_t)ty * CCL_BX;
+    const bool last_w = lane == 31 || !((sw >> (lane + 1)) & 1u);  // last block of its run
+    const bool last_b = lane == 31 || !((sb >> (lane + 1)) & 1u);
     par[2 * l] = 2 * (row0 + hw);
     par[2 * l + 1] = 2 * (row0 + hb) + 1;
     if (lane == 0) {
@@ -299,8 +301,6 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
             if (lane >= hw + o) aw |= yw;
             if (lane >= hb + o) ab |= yb;
         }
-        const bool last_w = lane == 31 || !((sw >> (lane + 1)) & 1u);
-        const bool last_b = lane == 31 || !((sb >> (lane + 1)) & 1u);
         const uint32_t up0 = row0 - CCL_BX;
         uint32_t ew = last_w ? (aw & ~((aw << 1) & row_runs[ty - 1][0])) : 0u;
         uint32_t eb = last_b ? (ab & ~((ab << 1) & row_runs[ty - 1][1])) : 0u;
@@ -310,9 +310,18 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __syncthreads();
     uint32_t rw = find_root_volatile((volatile uint32_t*)par, 2 * l);
     uint32_t rb = find_root_volatile((volatile uint32_t*)par, 2 * l + 1);
-    if (live) {
-        atomicAdd(&cnt[rw], __popc(L.info & 0xF));
-        atomicAdd(&cnt[rb], __popc(L.info & 0xF00));
+    // pixel counts per root: the blocks of a run share its root, so the
+    // run's last lane adds the run's count (segmented warp sum)
+    {
+        uint32_t cw = __popc(L.info & 0xF), cb = __popc(L.info & 0xF00);
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, cw, o), yb = __shfl_up_sync(0xFFFFFFFFu, cb, o);
+            if (lane >= hw + o) cw += yw;
+            if (lane >= hb + o) cb += yb;
+        }
+        if (last_w && cw) atomicAdd(&cnt[rw], cw);
+        if (last_b && cb) atomicAdd(&cnt[rb], cb);
     }
     __syncthreads();
     if (live) {
@@ -505,7 +514,9 @@ __global__ void __launch_bounds__(256) k_boundaries_dense(const __grid_constant_
 
 __global__ void __launch_bounds__(CCL_BX * 8) k_ccl_local_r8(const __grid_constant__ FrameSet fs) { ccl_local_impl<8>(fs); }
 __global__ void __launch_bounds__(CCL_BX * 16) k_ccl_local_r16(const __grid_constant__ FrameSet fs) { ccl_local_impl<16>(fs); }
+__global__ void __launch_bounds__(CCL_BX * 32) k_ccl_local_r32(const __grid_constant__ FrameSet fs) { ccl_local_impl<32>(fs); }
 __global__ void __launch_bounds__(256) k_ccl_border_r8(const __grid_constant__ FrameSet fs) { ccl_border_impl<8>(fs); }
 __global__ void __launch_bounds__(256) k_ccl_border_r16(const __grid_constant__ FrameSet fs) { ccl_border_impl<16>(fs); }
+__global__ void __launch_bounds__(256) k_ccl_border_r32(const __grid_constant__ FrameSet fs) { ccl_border_impl<32>(fs); }
 
 }  // namespace atag

@@ -164,7 +164,9 @@ def test_every_tuning_gives_identical_results_and_autotune_applies(tmp_path):
     for t in ({"ccl_tile_rows": 8, "boundary_tile_rows": 8, "small_cluster_max": 1024, "small_ctas_per_sm": 2,
                "large_ctas_divisor": 8, "index_ctas_per_sm": 4, "batch_lanes": 1},
               {"ccl_tile_rows": 16, "boundary_tile_rows": 8, "small_cluster_max": 2048, "small_ctas_per_sm": 6,
-               "large_ctas_divisor": 2, "index_ctas_per_sm": 16, "batch_lanes": 2}):
+               "large_ctas_divisor": 2, "index_ctas_per_sm": 16, "batch_lanes": 2},
+              {"ccl_tile_rows": 32, "boundary_tile_rows": 16, "small_cluster_max": 700, "small_ctas_per_sm": 8,
+               "large_ctas_divisor": 1, "index_ctas_per_sm": 8, "batch_lanes": 4}):
         det.set_tuning(**t)
         q, st = det.detect(frames)
         for a, b in zip(q, base):
