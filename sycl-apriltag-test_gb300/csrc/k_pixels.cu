@@ -229,18 +229,29 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __shared__ uint32_t row_runs[CCL_BY][2];  // S-link ballots of each tile row (255, 0 forest)
 
     // the tile's pixels plus a one-pixel halo (x0 - 1 .. x0 + 2 CCL_BX, y0 - 1
-    // ..), loaded as aligned 32-bit words (x0 and w are multiples of 4)
+    // ..), loaded as aligned 32-bit words (x0 and w are multiples of 4); all
+    // loads of a thread are issued before any is used
     {
         constexpr int WPR = (2 * CCL_BX + 8) / 4;  // words x0 - 4 .. x0 + 2 CCL_BX + 3
+        constexpr int NI = (PH * WPR + CCL_THREADS - 1) / CCL_THREADS;
         const uint32_t* thr32 = reinterpret_cast<const uint32_t*>(F.thr);
-        for (int i = threadIdx.x; i < PH * WPR; i += blockDim.x) {
-            const int r = i / WPR, k = i % WPR;
-            const int y = y0 - 1 + r, xw = x0 - 4 + 4 * k;
-            const uint32_t v = (y >= 0 && y < h && xw >= 0 && xw < w) ? thr32[((size_t)y * w + xw) / 4] : 0x7F7F7F7Fu;
+        uint32_t v[NI];
 #pragma unroll
-            for (int b = 0; b < 4; b++) {
-                const int c = xw + b - (x0 - 1);
-                if (c >= 0 && c < PW) pix[r][c] = (uint8_t)(v >> (8 * b));
+        for (int k = 0; k < NI; k++) {
+            const int i = threadIdx.x + k * CCL_THREADS, r = i / WPR, q = i % WPR;
+            const int y = y0 - 1 + r, xw = x0 - 4 + 4 * q;
+            v[k] = (i < PH * WPR && y >= 0 && y < h && xw >= 0 && xw < w) ? __ldg(thr32 + ((size_t)y * w + xw) / 4)
+                                                                          : 0x7F7F7F7Fu;
+        }
+#pragma unroll
+        for (int k = 0; k < NI; k++) {
+            const int i = threadIdx.x + k * CCL_THREADS, r = i / WPR, q = i % WPR;
+            if (i < PH * WPR) {
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const int c = 4 * q - 3 + b;  // xw + b - (x0 - 1)
+                    if (c >= 0 && c < PW) pix[r][c] = (uint8_t)(v[k] >> (8 * b));
+                }
             }
         }
     }
