@@ -221,15 +221,14 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
             stage[pos++] = stage_entry(0, cbase + (bit >> 2), r, bit & 3, 0);
         }
     }
-    __syncwarp();
-    // Then the warp takes its points 32 at a time: pair key, CTA table slot
-    // (one insert per distinct key of the round) and the per-pair sums of
-    // the round's points, merged into the table by one lane per key.
-    const uint32_t wbeg = __shfl_sync(0xFFFFFFFFu, pos0, 0);
-    const uint32_t wend = __shfl_sync(0xFFFFFFFFu, pos0 + (uint32_t)__popc(masks), 31);
-    for (uint32_t b0 = wbeg; b0 < wend; b0 += 32) {
+    __syncthreads();
+    // Then the CTA's warps take the staged points 32 at a time (round k of a
+    // warp covers points 32 (k W + warp) ..): pair key, CTA table slot (one
+    // insert per distinct key of the round) and the per-pair sums of the
+    // round's points, merged into the table by one lane per key.
+    for (uint32_t b0 = threadIdx.x & ~31u; b0 < nst; b0 += blockDim.x) {
         const uint32_t i = b0 + (uint32_t)lane;
-        const bool v = i < wend;
+        const bool v = i < nst;
         uint32_t e = v ? stage[i] : 0u;
         const int xo = (int)(e & 63), ro = (int)((e >> 6) & 15), t = (int)((e >> 10) & 3), c = xo + 1;
         const int rr = ro + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
