@@ -227,6 +227,7 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __shared__ uint32_t par[2 * CCL_THREADS];
     __shared__ uint32_t cnt[2 * CCL_THREADS];
     __shared__ uint32_t row_runs[CCL_BY][2];  // S-link ballots of each tile row (255, 0 forest)
+    __shared__ uint32_t ulist[CCL_BY][192];   // per row: unions with the row above (slot << 16 | slot)
 
     // the tile's pixels plus a one-pixel halo (x0 - 1 .. x0 + 2 CCL_BX, y0 - 1
     // ..), loaded as aligned 32-bit words (x0 and w are multiples of 4); all
@@ -315,8 +316,25 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         const uint32_t up0 = row0 - CCL_BX;
         uint32_t ew = last_w ? (aw & ~((aw << 1) & row_runs[ty - 1][0])) : 0u;
         uint32_t eb = last_b ? (ab & ~((ab << 1) & row_runs[ty - 1][1])) : 0u;
-        for (; ew; ew &= ew - 1) uf_union((volatile uint32_t*)par, 2 * (row0 + hw), 2 * (up0 + __ffs(ew) - 1));
-        for (; eb; eb &= eb - 1) uf_union((volatile uint32_t*)par, 2 * (row0 + hb) + 1, 2 * (up0 + __ffs(eb) - 1) + 1);
+        // the row's unions go to a list (a run touches at most its length
+        // + 2 blocks above, so a row has at most 96 per forest), which the
+        // warp's lanes then take one each
+        const uint32_t nu = (uint32_t)(__popc(ew) + __popc(eb));
+        uint32_t incl = nu;
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        uint32_t at = incl - nu;
+        for (; ew; ew &= ew - 1) ulist[ty][at++] = (2 * (row0 + hw)) << 16 | (2 * (up0 + __ffs(ew) - 1));
+        for (; eb; eb &= eb - 1) ulist[ty][at++] = (2 * (row0 + hb) + 1) << 16 | (2 * (up0 + __ffs(eb) - 1) + 1);
+        __syncwarp();
+        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        for (uint32_t k = lane; k < total; k += 32) {
+            const uint32_t e = ulist[ty][k];
+            uf_union((volatile uint32_t*)par, e >> 16, e & 0xFFFFu);
+        }
     }
     __syncthreads();
     uint32_t rw = find_root_volatile((volatile uint32_t*)par, 2 * l);
