@@ -375,7 +375,8 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
 // P/S of its left column and R (up-right) of its right column.  After the
 // local pass every slot points at its tile root, so a link is a union of
 // two tile roots; a lane skips a union that the lane before it (the
-// previous block of the same tile edge) makes too.
+// previous block of the same tile edge) makes too, and the warp's unions go
+// to a list that its lanes take one each.
 template <int CCL_BY>
 __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
     constexpr int CCL_BORDER_PER_TILE = CCL_BX + 2 * (CCL_BY - 1);
@@ -385,7 +386,8 @@ __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
     const int per_tile = CCL_BORDER_PER_TILE;
     const int total = ntx * nty * per_tile;
     volatile uint32_t* par = F.scratch;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ uint2 blist[8][8 * 32];  // per warp: the unions of one pass (8 per lane at most)
     bool ok = true;
     // warp-uniform trip count: lanes past the end take part in the votes
     for (int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < total; i0 += gridDim.x * blockDim.x) {
@@ -409,6 +411,10 @@ __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
         }
         const int ndx[4] = {-1, 0, 1, -1}, ndy[4] = {-1, -1, -1, 0};
         const uint32_t sid = (uint32_t)y * w + x;
+        const uint32_t rsw = live ? par[sid] : 0u, rsb = live ? par[sid + 1] : 0u;
+        // the lane's unions (up to 4 neighbours x 2 forests) into the warp's
+        // list, then one union per lane
+        uint32_t ka[8], kb[8], need = 0;
 #pragma unroll
         for (int n = 0; n < 4; n++) {
             const int nbx = bx + ndx[n], nby = by + ndy[n];
@@ -416,14 +422,34 @@ __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
             const bool cross = live && !(nbx >= tbx && nbx < tbx + CCL_BX && nby >= tby);
             const uint32_t nid = (uint32_t)(nby * 2) * w + nbx * 2;
             const bool lw = cross && (L.wmask & (1u << n)), lb = cross && (L.bmask & (1u << n));
-            const uint32_t aw = lw ? par[sid] : 0u, bw = lw ? par[nid] : 0u;
-            const uint32_t ab = lb ? par[sid + 1] : 0u, bb = lb ? par[nid + 1] : 0u;
-            const unsigned long long kw = lw ? ((unsigned long long)aw << 32 | bw) : ~0ull;
-            const unsigned long long kb = lb ? ((unsigned long long)ab << 32 | bb) : ~0ull;
-            const unsigned long long pw = __shfl_up_sync(0xFFFFFFFFu, kw, 1), pb = __shfl_up_sync(0xFFFFFFFFu, kb, 1);
-            if (lw && (lane == 0 || pw != kw)) ok &= uf_union(par, aw, bw);
-            if (lb && (lane == 0 || pb != kb)) ok &= uf_union(par, ab, bb);
+            ka[2 * n] = rsw;
+            kb[2 * n] = lw ? par[nid] : 0u;
+            ka[2 * n + 1] = rsb;
+            kb[2 * n + 1] = lb ? par[nid + 1] : 0u;
+            const unsigned long long kw = lw ? ((unsigned long long)ka[2 * n] << 32 | kb[2 * n]) : ~0ull;
+            const unsigned long long kk = lb ? ((unsigned long long)ka[2 * n + 1] << 32 | kb[2 * n + 1]) : ~0ull;
+            const unsigned long long pw = __shfl_up_sync(0xFFFFFFFFu, kw, 1), pb = __shfl_up_sync(0xFFFFFFFFu, kk, 1);
+            if (lw && (lane == 0 || pw != kw)) need |= 1u << (2 * n);
+            if (lb && (lane == 0 || pb != kk)) need |= 2u << (2 * n);
         }
+        const uint32_t nu = (uint32_t)__popc(need);
+        uint32_t incl = nu;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t at = incl - nu;
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (need & (1u << k)) blist[warp][at++] = make_uint2(ka[k], kb[k]);
+        __syncwarp();
+        const uint32_t nlist = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        for (uint32_t k = (uint32_t)lane; k < nlist; k += 32) {
+            const uint2 e = blist[warp][k];
+            ok &= uf_union(par, e.x, e.y);
+        }
+        __syncwarp();
     }
     if (!ok && F.counters) atomicOr(F.counters + CNT_STATUS, ATAG_DEVFLAG_UF_ITERATION_CAP);
 }
