@@ -553,6 +553,7 @@ __device__ __forceinline__ void cluster_sort(const FrameSet& fs, const uint32_t*
     constexpr uint32_t THREADS = LARGE ? CF_LARGE_THREADS : CF_SMALL_THREADS;
     extern __shared__ unsigned long long smem_keys[];
     __shared__ long long red_m[32][6];
+    __shared__ longlong2 lf_row[THREADS / 32][32][3];  // per warp: one row of LineFitPoints
     __shared__ uint32_t red32[33];
     __shared__ uint32_t s_item, s_flag;
     // radix counters of the global-memory sorts, after the padded key array
@@ -666,7 +667,22 @@ __device__ __forceinline__ void cluster_sort(const FrameSet& fs, const uint32_t*
                 const Moment m = i < n ? moment_of(at(i)) : Moment{0, 0, 0, 0, 0, 0};
                 const Moment in_seg = scan_moment<SEG>(m);
                 const Moment base = shfl_moment(off, (int)(r * (32 / SEG) + lane / SEG));
-                if (i < n) store_moment(F.line_fit + start + i, m_add(base, in_seg));
+                // the row's 32 LineFitPoints go out as 512-byte runs: each
+                // lane parks its 48 bytes in shared memory, then stores 16
+                // consecutive bytes of the row per instruction
+                const Moment lf = m_add(base, in_seg);
+                lf_row[w][lane][0] = make_longlong2(lf.Mx, lf.My);
+                lf_row[w][lane][1] = make_longlong2(lf.Mxx, lf.Myy);
+                lf_row[w][lane][2] = make_longlong2(lf.Mxy, lf.W);
+                __syncwarp();
+                const uint32_t r0 = c0 + r * 32;
+                longlong2* out = reinterpret_cast<longlong2*>(F.line_fit + start + r0);
+#pragma unroll
+                for (uint32_t q = 0; q < 4; q++) {
+                    const uint32_t piece = q * 32 + lane, pt = piece >> 2, f = piece & 3;
+                    if (r0 + pt < n) out[piece] = f < 3 ? lf_row[w][pt][f] : make_longlong2(0, 0);
+                }
+                __syncwarp();
             }
         }
         __syncthreads();

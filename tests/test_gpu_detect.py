@@ -52,8 +52,9 @@ def test_detect_small_and_edge_frames(det1080):
 
 def test_default_detector_skips_only_unread_intermediates(det1080):
     """A detector that does not keep intermediates gives the same quads,
-    labels and component sizes (at every label's root) as one that writes
-    the reference's full segmentation arrays."""
+    labels, component sizes (at every label's root), surviving clusters and
+    cluster points as one that writes the reference's full segmentation
+    arrays."""
     from atag.detector import Detector
     lean = Detector(1920, 1080)
     for seed in (5, 6):
@@ -65,6 +66,12 @@ def test_default_detector_skips_only_unread_intermediates(det1080):
         roots = np.unique(v_full["labels"].ravel() & 0x7FFFFFFF)
         assert np.array_equal(v_full["sizes"][roots], v_lean["sizes"][roots])
         assert np.array_equal(v_full["line_fit"], v_lean["line_fit"])
+        assert np.array_equal(v_full["cluster_keys"], v_lean["cluster_keys"])
+        assert np.array_equal(v_full["cluster_extents"], v_lean["cluster_extents"])
+        fields = [f for f in v_full["cluster_bounds"].dtype.names if f != "start"]
+        for f in fields:
+            assert np.array_equal(v_full["cluster_bounds"][f], v_lean["cluster_bounds"][f]), f
+        assert np.array_equal(v_full["cluster_points"], v_lean["cluster_points"])
 
 
 def test_detect_decimate2():
