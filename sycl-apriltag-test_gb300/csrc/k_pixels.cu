@@ -222,18 +222,19 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     const int bx0 = (blockIdx.x % ntx) * CCL_BX, by0 = (blockIdx.x / ntx) * CCL_BY;
     const int x0 = bx0 * 2, y0 = by0 * 2;
 
-    constexpr int PW = 2 * CCL_BX + 2, PH = 2 * CCL_BY + 1;
-    __shared__ uint8_t pix[PH][PW];  // rows y0-1.., cols x0-1..
+    constexpr int PH = 2 * CCL_BY + 1, WPR = (2 * CCL_BX + 8) / 4;
+    // rows y0 - 1 .., words of pixels x0 - 4 .. x0 + 2 CCL_BX + 3 (x0 and w
+    // are multiples of 4): pixel x of a row is byte x - x0 + 4
+    __shared__ uint32_t pixw[PH][WPR];
     __shared__ uint32_t par[2 * CCL_THREADS];
     __shared__ uint32_t cnt[2 * CCL_THREADS];
     __shared__ uint32_t row_runs[CCL_BY][2];  // S-link ballots of each tile row (255, 0 forest)
     __shared__ uint32_t ulist[CCL_BY][192];   // per row: unions with the row above (slot << 16 | slot)
 
     // the tile's pixels plus a one-pixel halo (x0 - 1 .. x0 + 2 CCL_BX, y0 - 1
-    // ..), loaded as aligned 32-bit words (x0 and w are multiples of 4); all
-    // loads of a thread are issued before any is used
+    // ..), loaded as aligned 32-bit words; all loads of a thread are issued
+    // before any is stored
     {
-        constexpr int WPR = (2 * CCL_BX + 8) / 4;  // words x0 - 4 .. x0 + 2 CCL_BX + 3
         constexpr int NI = (PH * WPR + CCL_THREADS - 1) / CCL_THREADS;
         const uint32_t* thr32 = reinterpret_cast<const uint32_t*>(F.thr);
         uint32_t v[NI];
@@ -246,14 +247,8 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         }
 #pragma unroll
         for (int k = 0; k < NI; k++) {
-            const int i = threadIdx.x + k * CCL_THREADS, r = i / WPR, q = i % WPR;
-            if (i < PH * WPR) {
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    const int c = 4 * q - 3 + b;  // xw + b - (x0 - 1)
-                    if (c >= 0 && c < PW) pix[r][c] = (uint8_t)(v[k] >> (8 * b));
-                }
-            }
+            const int i = threadIdx.x + k * CCL_THREADS;
+            if (i < PH * WPR) pixw[i / WPR][i % WPR] = v[k];
         }
     }
     const int tx = threadIdx.x % CCL_BX, ty = threadIdx.x / CCL_BX;
@@ -267,7 +262,8 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     BlockLinks L{0, 0, 0};
     if (live) {
         const int r0 = 2 * ty + 1, c0 = 2 * tx + 1;
-        L = block_links([&](int dy, int dx) { return (uint32_t)pix[r0 + dy][c0 + dx]; }, bx * 2, by * 2, w, h);
+        L = block_links([&](int dy, int dx) { return (uint32_t)reinterpret_cast<const uint8_t*>(pixw[r0 + dy])[c0 + dx + 3]; },
+                        bx * 2, by * 2, w, h);
     }
     // S links (left neighbour) inside the tile row, which is this warp: a run
     // of blocks that each link to their left neighbour points at its first
