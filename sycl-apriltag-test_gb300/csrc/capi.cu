@@ -364,7 +364,7 @@ atag_status atag_threshold_image(const uint8_t* grey, uint8_t* extrema, uint8_t*
     FrameDesc d = blank();
     d.width = (uint32_t)w; d.height = (uint32_t)h; d.factor = 1;
     d.grey = const_cast<uint8_t*>(grey); d.thr = thr; d.extrema = extrema; d.filtered_extrema = filtered;
-    size_t tiles = cdiv(w / 4, 32) * cdiv(h / 4, 8);
+    size_t tiles = cdiv(w / 4, 32) * cdiv(h / 4, 16);
     k_threshold<<<grid2(tiles, 1), 256, 0, (cudaStream_t)stream>>>(single(d), 5, (extrema || filtered) ? 1 : 0);
     LAUNCHED();
     return ATAG_OK;
@@ -640,7 +640,7 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
         LAUNCHED();
     }
     STAGE(2);
-    k_threshold<<<grid2(cdiv(mw / 4, 32) * cdiv(mh / 4, 8), n), 256, 0, s>>>(fs, p.min_white_black_diff, 0);
+    k_threshold<<<grid2(cdiv(mw / 4, 32) * cdiv(mh / 4, 16), n), 256, 0, s>>>(fs, p.min_white_black_diff, 0);
     LAUNCHED();
     STAGE(3);
     if (ccl_rows == 8) k_ccl_local_r8<<<grid2(tiles_ccl, n), 32 * 8, 0, s>>>(fs);

@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(256) k_reset_frames(const __grid_constant__ Fr
 // ---------------------------------------------------------------------------
 constexpr int BP_W = 64;                       // tile width; BP_H (8 or 16) rows is a tuning choice
 constexpr int BP_SW = BP_W + 2;
-constexpr int BP_LC = 128;                     // CTA hash-table entries (a tile has a few dozen pairs)
+constexpr int BP_LC = 64;                      // CTA hash-table entries (a tile has a few dozen pairs; more go straight to the frame's table)
 constexpr uint32_t BP_BIG = 0x40000000u, BP_VALUE = 0x3FFFFFFFu;
 
 struct PairTableSmem {

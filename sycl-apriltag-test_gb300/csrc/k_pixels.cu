@@ -43,11 +43,12 @@ __global__ void k_decimate(const __grid_constant__ FrameSet fs) {
 
 // ---------------------------------------------------------------------------
 // a1: threshold_image (threshold.cpp:8-95) in one kernel.  A CTA owns
-// TH_TX x TH_TY tiles of 4x4 pixels; it loads those plus a one-tile halo
-// into shared memory, takes each tile's min/max, dilates 3x3 (tiles outside
-// the image are neutral, which is the reference's clipping) and thresholds.
+// TH_TX x TH_TY (32 x 16) tiles of 4x4 pixels; it loads those plus a
+// one-tile halo into shared memory, takes each tile's min/max, dilates 3x3
+// (tiles outside the image are neutral, which is the reference's clipping)
+// and thresholds.
 // ---------------------------------------------------------------------------
-constexpr int TH_TX = 32, TH_TY = 8;
+constexpr int TH_TX = 32, TH_TY = 16;
 constexpr int TH_EX = TH_TX + 2, TH_EY = TH_TY + 2;
 
 __global__ void __launch_bounds__(256) k_threshold(const __grid_constant__ FrameSet fs,
