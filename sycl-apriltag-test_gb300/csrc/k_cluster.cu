@@ -689,7 +689,7 @@ __device__ __forceinline__ void cluster_sort(const FrameSet& fs, const uint32_t*
     }
 }
 
-__global__ void __launch_bounds__(CF_SMALL_THREADS) k_cluster_sort_small(const __grid_constant__ FrameSet fs,
+__global__ void __launch_bounds__(CF_SMALL_THREADS, 6) k_cluster_sort_small(const __grid_constant__ FrameSet fs,
                                                                         const uint32_t* __restrict__ work_offsets,
                                                                         uint32_t n_frames,
                                                                         uint32_t* __restrict__ work_counter,

@@ -458,7 +458,7 @@ __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
 // step, so four dependent loads are in flight at once.  The forest is final
 // here; the only concurrent writes replace a parent by its root, so any
 // value read is an ancestor.
-__global__ void __launch_bounds__(256) k_ccl_final(const __grid_constant__ FrameSet fs) {
+__global__ void __launch_bounds__(256, 8) k_ccl_final(const __grid_constant__ FrameSet fs) {
     const FrameDesc& F = fs.get(blockIdx.y);
     const int w = F.width, h = F.height;
     const int npx = w / 4, np = npx * (h / 2);  // block pairs (w % 4 == 0)
