@@ -131,9 +131,10 @@ def stage_bytes(stats, n_src_px):
     Cp = sum(int(s["n_peak_clusters"]) for s in stats)
     return {
         "threshold": 2 * N,                     # read grey, write thresholded
-        "ccl_local": N + 8 * N,                 # read thresholded; write 4 scratch + 4 size words per 2x2 block
+        "ccl_local": N + 4 * N,                 # read thresholded; write 2 parent + 2 size words per 2x2 block
         "ccl_border": 0,                        # latency: a few unions per tile edge
-        "ccl_final": 5 * N + 8 * N,             # read parents, sizes, pixels; write parents, sizes, labels
+        "ccl_final": 5 * N + 4 * N,             # read parents, sizes, pixels; write labels (batches keep
+                                                # no compressed forest or zero sizes)
         "boundaries_pairs": 4 * N + 8 * Pf,     # read labels; write the listed points (>= surviving ones)
         "pairs_finalize": 48 * C,
         "scatter_points": 8 * Pf + 8 * Pf,      # read listed points, write sort keys
