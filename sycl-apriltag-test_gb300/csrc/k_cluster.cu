@@ -197,21 +197,33 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     const int lane = threadIdx.x & 31;
     const int r = threadIdx.x / (BP_W / 4), cbase = (threadIdx.x % (BP_W / 4)) * 4;
     const int y = y0 + r;
-    uint32_t masks = 0;
+    // Bit j of cr/br (row r) and cb/bb (row r + 1) is the colour / size
+    // flag of the label at tile column cbase + j, i.e. pixel x0 + cbase - 1
+    // + j; the thread's pixel k is j = k + 1.  A pixel emits test t when it
+    // is in the image and big and the tested neighbour is big and of the
+    // other colour (BL also not when it duplicates the left pixel's BR):
+    // all four pixels' tests are computed at once on these bit rows.
+    uint32_t cr = 0, br = 0, cb = 0, bb = 0;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int xo = cbase + k, x = x0 + xo, c = xo + 1;
-        if (!(y < h && x > 0 && x < w) || !(lab[r][c] & BP_BIG)) continue;
-        const uint32_t cp = lab[r][c] & LABEL_PIXEL_MASK;
-        const bool dup = (lab[r][c - 1] & LABEL_PIXEL_MASK) != (lab[r + 1][c] & LABEL_PIXEL_MASK) &&
-                         (lab[r][c - 1] & BP_BIG) && (lab[r + 1][c] & BP_BIG);
-        uint32_t m = 0;
-        m |= ((lab[r][c + 1] & LABEL_PIXEL_MASK) != cp && (lab[r][c + 1] & BP_BIG)) ? 1u : 0u;
-        m |= (!dup && (lab[r + 1][c - 1] & LABEL_PIXEL_MASK) != cp && (lab[r + 1][c - 1] & BP_BIG)) ? 2u : 0u;
-        m |= ((lab[r + 1][c] & LABEL_PIXEL_MASK) != cp && (lab[r + 1][c] & BP_BIG)) ? 4u : 0u;
-        m |= ((lab[r + 1][c + 1] & LABEL_PIXEL_MASK) != cp && (lab[r + 1][c + 1] & BP_BIG)) ? 8u : 0u;
-        masks |= m << (4 * k);
+    for (int j = 0; j < 6; j++) {
+        const uint32_t a = lab[r][cbase + j], b = lab[r + 1][cbase + j];
+        cr |= (a >> 31) << j;
+        br |= ((a >> 30) & 1u) << j;
+        cb |= (b >> 31) << j;
+        bb |= ((b >> 30) & 1u) << j;
     }
+    uint32_t live = (y < h && x0 + cbase < w) ? 0xFu : 0u;  // w and x0 + cbase are multiples of 4
+    if (x0 + cbase == 0) live &= ~1u;                          // column 0 is never processed
+    live &= br >> 1;
+    const uint32_t cp = cr >> 1;
+    const uint32_t dup = (cr ^ (cb >> 1)) & br & (bb >> 1);
+    const uint32_t m0 = ((cr >> 2) ^ cp) & (br >> 2) & live;             // R
+    const uint32_t m1 = (cb ^ cp) & bb & ~dup & live;                    // BL
+    const uint32_t m2 = ((cb >> 1) ^ cp) & (bb >> 1) & live;             // B
+    const uint32_t m3 = ((cb >> 2) ^ cp) & (bb >> 2) & live;             // BR
+    // bit 4 k + t of masks: test t of pixel k
+    auto spread = [](uint32_t v) { return (v & 1u) | ((v & 2u) << 3) | ((v & 4u) << 6) | ((v & 8u) << 9); };
+    const uint32_t masks = spread(m0) | (spread(m1) << 1) | (spread(m2) << 2) | (spread(m3) << 3);
     uint32_t nst;
     const uint32_t pos0 = block_exclusive_scan_u32((uint32_t)__popc(masks), red, &nst);
     {
