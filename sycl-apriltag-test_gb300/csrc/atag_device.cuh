@@ -699,11 +699,14 @@ __device__ __forceinline__ void merge_sort_keys(const unsigned long long* __rest
                 }
             }
     const uint32_t tid = threadIdx.x;
+    // rounds whose pairs of runs belong to one warp only need that warp
+    // in step; wider rounds synchronise the CTA
 #pragma unroll 1
     for (uint32_t width = 1; width < (uint32_t)T; width <<= 1) {
 #pragma unroll
         for (int r = 0; r < K; r++) dst[kpad(tid * K + r)] = v[r];
-        __syncthreads();
+        if (2 * width <= 32) __syncwarp();
+        else __syncthreads();
         const uint32_t g0 = tid & ~(2 * width - 1), L = width * K;
         const uint32_t a0 = g0 * K, b0 = a0 + L, d = (tid - g0) * K;
         uint32_t lo = d > L ? d - L : 0u, hi = d < L ? d : L;
@@ -728,7 +731,8 @@ __device__ __forceinline__ void merge_sort_keys(const unsigned long long* __rest
                 b = ta ? b : nv;
             }
         }
-        __syncthreads();
+        if (2 * width <= 32) __syncwarp();
+        else __syncthreads();
     }
 #pragma unroll
     for (int r = 0; r < K; r++) dst[kpad(tid * K + r)] = v[r];
