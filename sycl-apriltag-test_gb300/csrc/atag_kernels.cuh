@@ -7,8 +7,8 @@ namespace atag {
 
 // Everything a kernel needs to know about one frame: its size and where its
 // buffers live in the workspace.  A batch is an array of these in device
-// memory; kernels pick their frame from blockIdx.y (pixel stages) or from a
-// flattened work index (cluster stages).
+// memory; kernels pick their frame from blockIdx.y (pixel stages),
+// blockIdx.x (boundary points) or a flattened work index (cluster stages).
 struct FrameDesc {
     // sizes
     uint32_t width, height;            // after decimation
@@ -64,6 +64,9 @@ struct FrameDesc {
     uint32_t quad_cap;
     atag_frame_stats* stats;
     uint32_t* counters;                // per-frame work counters (see Counter)
+    // DEAD_PAIRS keys (EMPTY = ~0) of pairs whose running point count is
+    // already above the cluster size limit; null when not tracked
+    unsigned long long* dead_pairs;
     // 1: write the reference's complete segmentation arrays (every parent
     // compressed to its root, block information words at odd rows, zero
     // sizes away from roots).  0 (fused batches): only what later stages
@@ -94,6 +97,8 @@ enum Counter : uint32_t {
     CNT_RUNS = 8,        // runs of up to CE_RUN points of one cluster
     CNT_COUNT = 9
 };
+
+constexpr uint32_t DEAD_PAIRS = 2;
 
 // Cluster-sort kernel shapes: most clusters are small and run several per SM
 // on 128 threads (up to 16 keys per thread), large ones get a 512-thread CTA

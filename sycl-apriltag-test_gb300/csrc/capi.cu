@@ -192,6 +192,7 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, bool ow
     f.cluster_work = (uint32_t*)take(4ull * c.cluster_cap);
     f.cluster_runs = (uint32_t*)take(4ull * c.cluster_cap);
     f.counters = (uint32_t*)take(4ull * CNT_COUNT);
+    f.dead_pairs = (unsigned long long*)take(8ull * DEAD_PAIRS);
     if (d) *d = f;
     return off;
 }
@@ -659,10 +660,12 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
     k_ccl_final<<<grid2(std::min<size_t>(cdiv((mw / 4) * (mh / 2), 256), 8192), n), 256, 0, s>>>(fs);
     LAUNCHED();
     STAGE(6);
+    // grid (frames, tiles): at most 64 x 512 tiles of a 4096 x 4096 frame,
+    // within gridDim.y's 65535
     if (bp_rows == 8)
-        k_boundaries_pairs_r8<<<grid2(cdiv(mw, 64) * cdiv(mh, 8), n), 16 * 8, 0, s>>>(fs, p.min_component_size);
+        k_boundaries_pairs_r8<<<dim3((unsigned)n, (unsigned)(cdiv(mw, 64) * cdiv(mh, 8))), 16 * 8, 0, s>>>(fs, p.min_component_size);
     else
-        k_boundaries_pairs_r16<<<grid2(cdiv(mw, 64) * cdiv(mh, 16), n), 16 * 16, 0, s>>>(fs, p.min_component_size);
+        k_boundaries_pairs_r16<<<dim3((unsigned)n, (unsigned)(cdiv(mw, 64) * cdiv(mh, 16))), 16 * 16, 0, s>>>(fs, p.min_component_size);
     LAUNCHED();
     STAGE(7);
     k_pairs_finalize<<<(unsigned)n, 1024, 0, s>>>(fs, p, (uint32_t)tu.small_cluster_max);

@@ -48,6 +48,7 @@ __global__ void __launch_bounds__(256) k_reset_frames(const __grid_constant__ Fr
         F.pair_cluster[i] = INVALID;
     }
     if (blockIdx.x == 0 && threadIdx.x < CNT_COUNT) F.counters[threadIdx.x] = 0u;
+    if (blockIdx.x == 0 && threadIdx.x < DEAD_PAIRS && F.dead_pairs) F.dead_pairs[threadIdx.x] = EMPTY_KEY;
 }
 
 // ---------------------------------------------------------------------------
@@ -133,11 +134,15 @@ template <int BP_H>
 __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32_t min_size) {
     constexpr int BP_SH = BP_H + 1;
     constexpr int BP_STAGE = BP_W * BP_H * 4;  // at most 4 points per pixel
-    const FrameDesc& F = fs.get(blockIdx.y);
+    // frame from blockIdx.x, tile from blockIdx.y: CTAs are dispatched
+    // frame-fastest, so the tiles in flight at once span every frame of the
+    // batch and a frame's later tiles start after its first ones published
+    // their over-limit pairs
+    const FrameDesc& F = fs.get(blockIdx.x);
     const int w = F.width, h = F.height;
     const int ntx = (w + BP_W - 1) / BP_W, nty = (h + BP_H - 1) / BP_H;
-    if ((int)blockIdx.x >= ntx * nty) return;
-    const int x0 = (blockIdx.x % ntx) * BP_W, y0 = (blockIdx.x / ntx) * BP_H;
+    if ((int)blockIdx.y >= ntx * nty) return;
+    const int x0 = (blockIdx.y % ntx) * BP_W, y0 = (blockIdx.y / ntx) * BP_H;
     uint32_t* status = F.counters + CNT_STATUS;
 
     // labels of the tile and its halo; bit 30 (free: label values are
@@ -147,6 +152,8 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     __shared__ uint32_t stage[BP_STAGE];
     __shared__ uint32_t red[33];
     __shared__ uint32_t s_base;
+    __shared__ unsigned long long s_dead[DEAD_PAIRS];
+    const bool track_dead = !F.stage_outputs && F.dead_pairs;
 
     // labels of the tile (16-byte loads of four) and its halo columns, then
     // the size of each label's component: all label loads of a thread are
@@ -183,6 +190,9 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
             }
         }
     }
+    // pairs that earlier tiles already pushed over the cluster size limit
+    // (a snapshot: a pair published later is simply processed in full)
+    if (threadIdx.x < DEAD_PAIRS) s_dead[threadIdx.x] = track_dead ? __ldcg(F.dead_pairs + threadIdx.x) : EMPTY_KEY;
     for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
         T.key[i] = EMPTY_KEY;
         T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
@@ -248,6 +258,14 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         const uint32_t lp = p & BP_VALUE, lq = q & BP_VALUE;
         const int dir = (q & LABEL_PIXEL_MASK) > (p & LABEL_PIXEL_MASK) ? 1 : 0;
         const unsigned long long key = v ? (((unsigned long long)min(lp, lq) << 32) | max(lp, lq)) : EMPTY_KEY;
+        // a round whose points all belong to pairs already over the limit
+        // contributes nothing: its points are neither aggregated nor listed
+        static_assert(DEAD_PAIRS == 2, "the test below reads both entries");
+        const bool dead = v && (key == s_dead[0] || key == s_dead[1]);
+        if (__all_sync(0xFFFFFFFFu, dead || !v)) {
+            if (v) stage[i] = e | STAGE_DIRECT;
+            continue;
+        }
         const unsigned m = __match_any_sync(0xFFFFFFFFu, key);
         const int leader = __ffs(m) - 1;
         int ls = 0;
@@ -306,6 +324,11 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         uint32_t old = global_flush(F, gs, T.cnt[i], T.xmin[i], T.xmax[i], T.ymin[i], T.ymax[i], T.gx[i], T.gy[i],
                                     T.pxgx[i]);
         T.gslot[i] = (old + T.cnt[i] > max_pixels) ? INVALID : gs;
+        // the flush that crosses the limit publishes the pair, so that later
+        // tiles skip its points (its count only grows: it stays rejected)
+        if (track_dead && old <= max_pixels && old + T.cnt[i] > max_pixels)
+            for (uint32_t d = 0; d < DEAD_PAIRS; d++)
+                if (atomicCAS(F.dead_pairs + d, EMPTY_KEY, key) == EMPTY_KEY) break;
     }
     __syncthreads();
 
