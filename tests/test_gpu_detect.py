@@ -74,6 +74,28 @@ def test_default_detector_skips_only_unread_intermediates(det1080):
         assert np.array_equal(v_full["cluster_points"], v_lean["cluster_points"])
 
 
+def test_skipping_pairs_over_the_size_limit_changes_nothing():
+    """In a lean batch the boundary tiles skip the points of pairs that
+    earlier tiles already pushed over ValidBlobFilter's size limit (these
+    frames have two to four such pairs, the largest of 1.1-1.2 M points; the
+    frame's list holds two).  Quads and every per-frame count equal those of
+    a detector that keeps the full per-pair sums."""
+    from atag.detector import Detector
+    imgs = [torch.from_numpy(synth_frame("1080p", 20 + i)).cuda() for i in range(12)]
+    lean = Detector(1920, 1080, max_frames=len(imgs), max_total_pixels=len(imgs) * 1920 * 1080)
+    full = Detector(1920, 1080, max_frames=len(imgs), max_total_pixels=len(imgs) * 1920 * 1080,
+                    keep_intermediates=True)
+    q_lean, st_lean = lean.detect(imgs)
+    q_full, st_full = full.detect(imgs)
+    fields = ("n_points", "n_pairs", "n_clusters", "n_cluster_points", "n_corners", "n_peak_clusters",
+              "n_fitted", "n_quads", "status")
+    for i in range(len(imgs)):
+        assert int(st_lean[i]["status"]) == 0
+        assert len(q_full[i]) > 0 and q_lean[i].tobytes() == q_full[i].tobytes()
+        for f in fields:
+            assert int(st_lean[i][f]) == int(st_full[i][f]), (i, f)
+
+
 def test_detect_decimate2():
     from atag import lib
     from atag.detector import Detector
