@@ -349,13 +349,16 @@ atag_status atag_use_device(int ordinal);
 
 atag_status atag_detector_views(const atag_detector *det, size_t frame, atag_frame_views *out);
 
-/* Segmentation arrays of later detect calls.  By default a detector writes
- * only what its own later stages read: labels in full, parents at even rows
- * and component sizes at the root slots.  keep != 0 makes it also write the
- * rest of the reference's scratch and sizes arrays (parents compressed to
- * roots, block information words, zero sizes away from roots:
- * src/segmentation.cpp:309-389), as atag_image_segmentation does, so that
- * atag_detector_views shows them in full. */
+/* Intermediates of later detect calls.  By default a detector writes only
+ * what its own later stages read: labels in full, parents at even rows and
+ * component sizes at the root slots; and once a pair's point count is over
+ * ValidBlobFilter's maximum, its later points are no longer summed (its
+ * pair_count, pair_bbox, pair_gsum and pair_pxgx stop growing; it is
+ * rejected all the same).  keep != 0 makes it also write the rest of the
+ * reference's scratch and sizes arrays (parents compressed to roots, block
+ * information words, zero sizes away from roots:
+ * src/segmentation.cpp:309-389), as atag_image_segmentation does, and sum
+ * every pair in full, so that atag_detector_views shows them complete. */
 atag_status atag_detector_keep_intermediates(atag_detector *det, int keep);
 
 /* ------------------------------------------------------------------ */

@@ -51,8 +51,10 @@ class Detector:
 
     def keep_intermediates(self, keep: bool = True):
         """With keep, later calls also write the reference's full scratch and
-        sizes arrays (zeros away from component roots), which `views` shows;
-        by default only what the later stages read is written."""
+        sizes arrays (zeros away from component roots) and sum every pair in
+        full, which `views` shows; by default only what the later stages read
+        is written, and pairs already over the cluster size limit stop being
+        summed."""
         lib.check(self.L.atag_detector_keep_intermediates(self.handle, 1 if keep else 0),
                   "atag_detector_keep_intermediates")
 

@@ -10,7 +10,9 @@
 //      them per cluster pair in a shared-memory hash table (warp-level
 //      reductions first), merges the per-pair ClusterBounds sums into a
 //      per-frame global hash table with one set of atomics per (CTA, pair),
-//      and appends its points, tagged with their pair slot, to a list;
+//      and appends its points, tagged with their pair slot, to a list
+//      (in batches, points of pairs that earlier tiles already pushed over
+//      the cluster size limit are skipped);
 //   2. k_pairs_finalize: one CTA per frame sorts the distinct pair keys
 //      (hundreds to a few thousand), applies ValidBlobFilter and assigns
 //      each surviving pair its cluster index and extent;
