@@ -13,7 +13,10 @@ resident in HBM.  Also measured:
           overlap the previous step's detection;
   stages  per-stage device times (CUDA events recorded by the detector on
           its stream between stages) -> roofline of the dominant kernel;
-  cpu     the CPU oracle (C restatement of the reference) on the host cores.
+  cpu     the CPU oracle (C restatement of the reference) on the host cores;
+  mixed / refine / pose / serving
+          the batching, differentiation (corner refinement forward + adjoint),
+          tag pose and serving configurations.
 `--impl reference` times the reference's CPU path instead (the oracle port:
 the reference's SYCL/oneDPL toolchain does not exist here).
 """
@@ -242,7 +245,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mixed", type=int, default=64, help="frames of the mixed-resolution batch (0 = skip)")
-    ap.add_argument("--refine-quads", type=int, default=4096, help="quads of the refinement step (0 = skip)")
+    ap.add_argument("--refine-quads", type=int, default=4096, help="quads of the refinement and pose steps (0 = skip)")
     ap.add_argument("--serving-seconds", type=float, default=5.0, help="length of the serving run (0 = skip)")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
@@ -465,7 +468,7 @@ def main():
         del detm, gm
 
     # --- corner refinement: forward + hand-written adjoint on 4096 quads
-    refine_line = None
+    refine_line = pose_line = None
     if args.refine_quads > 0:
         from atag import refine
         g = torch.Generator(device="cpu").manual_seed(3)
@@ -489,6 +492,23 @@ def main():
         rms = a.elapsed_time(b) / args.steps
         refine_line = {"quads": nq, "samples_per_quad": 256, "ms_fwd_bwd": rms,
                        "quads_per_s": nq / (rms / 1000.0)}
+
+        # --- tag pose of the same quads (FP64 homography + Levenberg-Marquardt)
+        from atag import pose
+        cam = (1000.0, 1000.0, W / 2.0, H / 2.0)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                poses = pose.estimate_pose(quads_c, *cam, 0.16, stream=stream)
+            a.record(stream)
+            for _ in range(args.steps):
+                poses = pose.estimate_pose(quads_c, *cam, 0.16, stream=stream)
+            b.record(stream)
+        b.synchronize()
+        pms = a.elapsed_time(b) / args.steps
+        pn = pose.to_numpy(poses)
+        pose_line = {"quads": nq, "ms": pms, "poses_per_s": nq / (pms / 1000.0), "max_iterations": 20,
+                     "mean_iterations": float(pn["iterations"].mean()),
+                     "max_reproj_px": float(pn["reproj_rms"].max()), "degenerate": int((pn["status"] & 2).sum())}
 
     # --- serving: 8 cameras (4 x 720p60, 4 x 1080p30), Poisson arrivals
     serving_line = None
@@ -538,6 +558,7 @@ def main():
         "batched_vs_plain": value / world / plain["frames_per_s"] if plain else None,
         "mixed_batch": mixed,
         "refine": refine_line,
+        "pose": pose_line,
         "serving": serving_line,
         "tuning": tuning["tuning"] if tuning else None,
         "roofline": roofline,

@@ -386,6 +386,44 @@ atag_status atag_refine_backward(const float *d_image, size_t width, size_t heig
                                  float *d_grad_corners, float *d_grad_samples, float *d_grad_image,
                                  atag_stream_t stream);
 
+/* ------------------------------------------------------------------ */
+/* Tag pose from quad corners (no counterpart in the reference; a      */
+/* downstream consumer of its quads).                                  */
+/* ------------------------------------------------------------------ */
+/* Corner i of a quad is taken as the image of the tag-plane point
+ * (tag_size / 2) * c_i, c = (-1,-1), (1,-1), (1,1), (-1,1), z = 0: for a tag
+ * seen upright from the front (tag z axis pointing away from the camera)
+ * that is top-left, top-right, bottom-right, bottom-left, clockwise on a
+ * y-down image.  A quad wound the other way is taken in the order 0, 3, 2,
+ * 1 and flagged.  Without decoding the tag's rotation by multiples of 90
+ * degrees is unknown; the corner order fixes it.  Pinhole camera without
+ * distortion: x = fx X / Z + cx, y = fy Y / Z + cy; camera point
+ * = R * tag point + t. */
+#define ATAG_POSE_REORDERED 0x1u  /* corners were wound the other way         */
+#define ATAG_POSE_DEGENERATE 0x2u /* no homography or no pose in front of the
+                                     camera; R, t, H and reproj_rms are zero   */
+typedef struct atag_pose {
+    double R[9];         /* row-major rotation, tag frame -> camera frame   */
+    double t[3];         /* translation, in the unit of tag_size            */
+    double H[9];         /* row-major homography tag plane (X, Y, 1) ->
+                            pixel (x, y, 1) of the refined pose, H[8] = 1   */
+    double reproj_rms;   /* RMS corner reprojection error in pixels         */
+    uint32_t iterations; /* accepted Levenberg-Marquardt steps              */
+    uint32_t status;     /* ATAG_POSE_* bits                                */
+} atag_pose;
+
+/* One pose per quad, FP64: homography of the unit square onto the quad in
+ * closed form, initial pose from its columns (polar-orthogonalised
+ * rotation), then up to max_iterations Levenberg-Marquardt trials on the
+ * pixel reprojection error of the four corners (20 is plenty; 0 keeps the
+ * homography's pose).  Corner q's eight floats (x0, y0,
+ * .. x3, y3) start at byte q * corner_stride of d_corners: 40 for an array
+ * of atag_quad_corners, 32 for packed corners such as atag_refine_forward's
+ * output. */
+atag_status atag_estimate_pose(const float *d_corners, size_t corner_stride, size_t n_quads, double fx,
+                               double fy, double cx, double cy, double tag_size, uint32_t max_iterations,
+                               atag_pose *d_poses, atag_stream_t stream);
+
 /* Launch shapes of the detector's kernels.  Every choice gives the same
  * results; only the speed changes.  atag_detector_create starts from the
  * defaults below; the autotuner (sycl-apriltag-test_gb300/atag/autotune.py)

@@ -104,6 +104,15 @@ struct CornerRefine {
     }
 };
 
+// Tag pose per quad (no counterpart in the reference): corner_stride is
+// sizeof(QuadCorners) for detector output, 8 floats for packed corners.
+inline atag_status estimate_pose(cudaStream_t q, const float* corners, size_t corner_stride, size_t n_quads,
+                                 double fx, double fy, double cx, double cy, double tag_size, atag_pose* poses,
+                                 uint32_t max_iterations = 20) {
+    return atag_estimate_pose(corners, corner_stride, n_quads, fx, fy, cx, cy, tag_size, max_iterations, poses,
+                              as_stream(q));
+}
+
 // RAII owner of an atag_detector (the whole path of src/main.cpp:322-1024).
 class Detector {
 public:

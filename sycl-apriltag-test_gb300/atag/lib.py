@@ -22,6 +22,7 @@ _P = ctypes.c_void_p
 _SZ = ctypes.c_size_t
 _U32 = ctypes.c_uint32
 _ST = ctypes.c_int
+_D = ctypes.c_double
 
 _SIGNATURES = {
     "atag_config_default": (None, [ctypes.POINTER(Config)]),
@@ -53,6 +54,7 @@ _SIGNATURES = {
     "atag_detector_set_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
     "atag_refine_forward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P]),
     "atag_refine_backward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P, _P, _P]),
+    "atag_estimate_pose": (_ST, [_P, _SZ, _SZ, _D, _D, _D, _D, _D, _U32, _P, _P]),
 }
 STAGE_COUNT = 15
 

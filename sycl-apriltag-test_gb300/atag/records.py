@@ -23,6 +23,10 @@ FRAME_STATS = np.dtype([(n, "<u4") for n in ("width", "height", "n_points", "n_p
                                               "n_cluster_points", "n_corners", "n_peak_clusters",
                                               "n_fitted", "n_quads", "status")] + [("reserved", "<u4", (5,))])
 
+POSE = np.dtype([("R", "<f8", (3, 3)), ("t", "<f8", (3,)), ("H", "<f8", (3, 3)), ("reproj_rms", "<f8"),
+                 ("iterations", "<u4"), ("status", "<u4")])
+
+assert POSE.itemsize == 184
 assert BOUNDARY_POINT.itemsize == 4 and CLUSTER_POINT.itemsize == 8 and CLUSTER_EXTENTS.itemsize == 8
 assert CLUSTER_BOUNDS.itemsize == 32 and LINE_FIT_POINT.itemsize == 64 and CORNER.itemsize == 12
 assert FITTED_QUAD.itemsize == 272 and QUAD_CORNERS.itemsize == 40 and FRAME_STATS.itemsize == 64
