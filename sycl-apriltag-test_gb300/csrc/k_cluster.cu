@@ -215,7 +215,23 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     // is in the image and big and the tested neighbour is big and of the
     // other colour (BL also not when it duplicates the left pixel's BR):
     // all four pixels' tests are computed at once on these bit rows.
-    uint32_t cr = 0, br = 0, cb = 0, bb = 0;
+    // dr/db: the label is one of the two labels of the frame's first pair
+    // known to be over the cluster size limit.  A pair joins a white label
+    // (colour bit | an even root slot) and a black one (an odd root slot, or
+    // label 0 of pixels that are neither 0 nor 255); a boundary point whose
+    // two labels are both in the set is a point of that pair.
+    uint32_t dW = 0xFFFFFFFFu, dK = 0xFFFFFFFFu;
+    {
+        const uint32_t kA = (uint32_t)(s_dead[0] >> 32), kB = (uint32_t)s_dead[0];
+        if ((kA ^ kB) & 1u) {
+            dW = LABEL_PIXEL_MASK | ((kA & 1u) ? kB : kA);
+            dK = (kA & 1u) ? kA : kB;
+        } else if (kA == 0u) {
+            dW = LABEL_PIXEL_MASK | kB;
+            dK = 0u;
+        }
+    }
+    uint32_t cr = 0, br = 0, cb = 0, bb = 0, dr = 0, db = 0;
 #pragma unroll
     for (int j = 0; j < 6; j++) {
         const uint32_t a = lab[r][cbase + j], b = lab[r + 1][cbase + j];
@@ -223,6 +239,9 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         br |= ((a >> 30) & 1u) << j;
         cb |= (b >> 31) << j;
         bb |= ((b >> 30) & 1u) << j;
+        const uint32_t al = a & ~BP_BIG, bl = b & ~BP_BIG;
+        dr |= (uint32_t)(al == dW || al == dK) << j;
+        db |= (uint32_t)(bl == dW || bl == dK) << j;
     }
     uint32_t live = (y < h && x0 + cbase < w) ? 0xFu : 0u;  // w and x0 + cbase are multiples of 4
     if (x0 + cbase == 0) live &= ~1u;                          // column 0 is never processed
@@ -236,11 +255,18 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     // bit 4 k + t of masks: test t of pixel k
     auto spread = [](uint32_t v) { return (v & 1u) | ((v & 2u) << 3) | ((v & 4u) << 6) | ((v & 8u) << 9); };
     const uint32_t masks = spread(m0) | (spread(m1) << 1) | (spread(m2) << 2) | (spread(m3) << 3);
-    uint32_t nst;
-    const uint32_t pos0 = block_exclusive_scan_u32((uint32_t)__popc(masks), red, &nst);
+    // points of that pair are counted but not staged
+    const uint32_t dp = dr >> 1;
+    const uint32_t d0 = dp & (dr >> 2), d1 = dp & db, d2 = dp & (db >> 1), d3 = dp & (db >> 2);
+    const uint32_t staged = masks & ~(spread(d0) | (spread(d1) << 1) | (spread(d2) << 2) | (spread(d3) << 3));
+    // one scan of both counts (a CTA has at most 4096 points: no carry)
+    uint32_t both;
+    const uint32_t pos0 =
+        block_exclusive_scan_u32((uint32_t)__popc(staged) | ((uint32_t)__popc(masks) << 16), red, &both) & 0xFFFFu;
+    const uint32_t nst = both & 0xFFFFu, nall = both >> 16;
     {
         uint32_t pos = pos0;
-        for (uint32_t mm = masks; mm; mm &= mm - 1) {
+        for (uint32_t mm = staged; mm; mm &= mm - 1) {
             const int bit = __ffs(mm) - 1;
             stage[pos++] = stage_entry(0, cbase + (bit >> 2), r, bit & 3, 0);
         }
@@ -346,7 +372,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     const uint32_t off = block_exclusive_scan_u32(nlive, red, &total);
     if (threadIdx.x == 0) {
         uint32_t b = total ? atomicAdd(F.counters + CNT_POINTS, total) : 0u;
-        if (nst) atomicAdd(F.counters + CNT_ALLPOINTS, nst);
+        if (nall) atomicAdd(F.counters + CNT_ALLPOINTS, nall);
         if ((unsigned long long)b + total > F.point_cap) atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
         s_base = b;
     }
