@@ -80,6 +80,9 @@ def test_calls_without_device_return_status(monkeypatch):
     assert L.atag_last_error()
     st = L.atag_threshold_image(None, None, None, None, 64, 64, None)
     assert st == 5
+    st = L.atag_estimate_pose(None, 32, 4, 1000.0, 1000.0, 960.0, 540.0, 0.16, 20, None, None)
+    assert st == 5
+    assert L.atag_refine_forward(None, 64, 64, None, 1, None, None, None, None) == 5
 
 
 def test_cpp_header_compiles_against_the_c_abi(tmp_path):
