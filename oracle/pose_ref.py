@@ -170,7 +170,8 @@ def project(R, t, cam, tag_size):
 def random_poses(n, seed, tag_size=0.16, max_angle_deg=60.0, dist=(0.4, 4.0), cam=(1000.0, 1000.0, 960.0, 540.0),
                  size=(1920, 1080)):
     """Seeded poses of a tag facing the camera (tilted up to max_angle_deg,
-    any roll) whose corners fall inside the image."""
+    any roll; its front seen, i.e. its z axis along the viewing ray) whose
+    corners fall inside the image."""
     rng = np.random.default_rng(seed)
     out = []
     while len(out) < n:
@@ -182,6 +183,8 @@ def random_poses(n, seed, tag_size=0.16, max_angle_deg=60.0, dist=(0.4, 4.0), ca
         R = so3_exp(ax * tilt) @ so3_exp(np.array([0.0, 0.0, rng.uniform(-math.pi, math.pi)]))
         z = rng.uniform(*dist)
         t = np.array([rng.uniform(-0.4, 0.4) * z, rng.uniform(-0.25, 0.25) * z, z])
+        if not R[:, 2] @ t > 0.0:
+            continue
         c = project(R, t, cam, tag_size)
         if np.all(c[:, 0] > 0) and np.all(c[:, 0] < size[0]) and np.all(c[:, 1] > 0) and np.all(c[:, 1] < size[1]):
             out.append((R, t, c))

@@ -79,3 +79,21 @@ def test_so3_exp_is_a_rotation_by_the_angle():
     assert abs(_rot_err(np.eye(3), R) - np.linalg.norm(w)) < 1e-12
     assert np.allclose(R @ w, w, atol=1e-14)
     assert np.allclose(project(np.eye(3), [0, 0, 1.0], CAM, TAG)[0], [960 - 80, 540 - 80])
+
+
+def test_steep_tilts_and_anisotropic_cameras():
+    cam = (1400.0, 1250.0, 900.0, 560.0)
+    for R, t, c in random_poses(100, seed=5, max_angle_deg=80.0, cam=cam, dist=(0.3, 2.0)):
+        p = estimate_pose_one(c, cam, TAG)
+        assert p["status"] == 0
+        assert _rot_err(p["R"], R) < 1e-8
+        assert np.linalg.norm(p["t"] - t) < 1e-8 * np.linalg.norm(t)
+        assert p["reproj_rms"] < 1e-8
+
+
+def test_tag_size_scales_translation_only():
+    R, t, c = random_poses(1, seed=6)[0]
+    a = estimate_pose_one(c, CAM, TAG)
+    b = estimate_pose_one(c, CAM, 2 * TAG)
+    assert _rot_err(a["R"], b["R"]) < 1e-10
+    assert np.allclose(b["t"], 2 * a["t"], rtol=1e-10)
