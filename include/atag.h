@@ -424,6 +424,46 @@ atag_status atag_estimate_pose(const float *d_corners, size_t corner_stride, siz
                                double fy, double cx, double cy, double tag_size, uint32_t max_iterations,
                                atag_pose *d_poses, atag_stream_t stream);
 
+/* ------------------------------------------------------------------ */
+/* Reading tags: the bit grid of each quad against a code family.       */
+/* The reference passes each quad to the AprilTag library's             */
+/* quad_decode_task with tag36h11 (src/quad_decoding.cpp:46-128); that  */
+/* library and its family tables are not in the reference tree, so the */
+/* family's codes are an argument.                                      */
+/* ------------------------------------------------------------------ */
+#define ATAG_DECODE_REORDERED 0x1u    /* corners were wound the other way        */
+#define ATAG_DECODE_DEGENERATE 0x2u   /* the corners admit no homography         */
+#define ATAG_DECODE_LOW_CONTRAST 0x4u /* white ring minus black border below
+                                         min_contrast: no bits read               */
+typedef struct atag_decoded {
+    uint64_t code;      /* bits read, cell (r, c) at bit D*D-1-(D r + c), rotation 0 */
+    int32_t id;         /* index of the matched code, -1 if none within max_hamming */
+    uint32_t hamming;   /* distance to the nearest code over the four rotations     */
+    uint32_t rotation;  /* quarter turns of the read grid that give the match       */
+    uint32_t status;    /* ATAG_DECODE_* bits                                       */
+    float black, white; /* mean grey of the black border and of the ring outside it */
+    float margin;       /* smallest |sample - threshold| over the data cells        */
+    uint32_t reserved;
+} atag_decoded;
+
+/* Tag layout: data_side x data_side data cells (2..8) inside a one-cell
+ * black border inside a white quiet zone; the quad is the outer edge of the
+ * black border, its corners as for atag_estimate_pose (a quad wound the
+ * other way is read mirrored back and flagged).  Per quad: the projective
+ * map of the unit square onto the quad in closed form, bilinear samples at
+ * cell centres (pixel centres at integer coordinates), threshold halfway
+ * between the mean of the black border cells and the mean of the ring of
+ * cells just outside it, bit = sample > threshold; then the code of d_codes
+ * (n_codes 64-bit codes, bit D*D-1-(D r + c) = cell r, c) and quarter turn
+ * with the smallest Hamming distance (first on ties), accepted at most
+ * max_hamming.  corner_stride as for atag_estimate_pose (40: detector
+ * output); pitch 0 = width. */
+atag_status atag_decode_quads(const uint8_t *d_image, size_t width, size_t height, size_t pitch,
+                              const float *d_corners, size_t corner_stride, size_t n_quads,
+                              const uint64_t *d_codes, size_t n_codes, uint32_t data_side,
+                              uint32_t max_hamming, double min_contrast, atag_decoded *d_out,
+                              atag_stream_t stream);
+
 /* Launch shapes of the detector's kernels.  Every choice gives the same
  * results; only the speed changes.  atag_detector_create starts from the
  * defaults below; the autotuner (sycl-apriltag-test_gb300/atag/autotune.py)

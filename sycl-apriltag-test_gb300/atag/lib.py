@@ -55,6 +55,7 @@ _SIGNATURES = {
     "atag_refine_forward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P]),
     "atag_refine_backward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P, _P, _P]),
     "atag_estimate_pose": (_ST, [_P, _SZ, _SZ, _D, _D, _D, _D, _D, _U32, _P, _P]),
+    "atag_decode_quads": (_ST, [_P, _SZ, _SZ, _SZ, _P, _SZ, _SZ, _P, _SZ, _U32, _U32, _D, _P, _P]),
 }
 STAGE_COUNT = 15
 

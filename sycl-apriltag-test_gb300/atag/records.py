@@ -26,7 +26,10 @@ FRAME_STATS = np.dtype([(n, "<u4") for n in ("width", "height", "n_points", "n_p
 POSE = np.dtype([("R", "<f8", (3, 3)), ("t", "<f8", (3,)), ("H", "<f8", (3, 3)), ("reproj_rms", "<f8"),
                  ("iterations", "<u4"), ("status", "<u4")])
 
-assert POSE.itemsize == 184
+DECODED = np.dtype([("code", "<u8"), ("id", "<i4"), ("hamming", "<u4"), ("rotation", "<u4"), ("status", "<u4"),
+                    ("black", "<f4"), ("white", "<f4"), ("margin", "<f4"), ("reserved", "<u4")])
+
+assert POSE.itemsize == 184 and DECODED.itemsize == 40
 assert BOUNDARY_POINT.itemsize == 4 and CLUSTER_POINT.itemsize == 8 and CLUSTER_EXTENTS.itemsize == 8
 assert CLUSTER_BOUNDS.itemsize == 32 and LINE_FIT_POINT.itemsize == 64 and CORNER.itemsize == 12
 assert FITTED_QUAD.itemsize == 272 and QUAD_CORNERS.itemsize == 40 and FRAME_STATS.itemsize == 64
