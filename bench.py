@@ -14,9 +14,9 @@ resident in HBM.  Also measured:
   stages  per-stage device times (CUDA events recorded by the detector on
           its stream between stages) -> roofline of the dominant kernel;
   cpu     the CPU oracle (C restatement of the reference) on the host cores;
-  mixed / refine / pose / serving
+  mixed / refine / pose / decode / serving
           the batching, differentiation (corner refinement forward + adjoint),
-          tag pose and serving configurations.
+          tag pose, tag reading and serving configurations.
 `--impl reference` times the reference's CPU path instead (the oracle port:
 the reference's SYCL/oneDPL toolchain does not exist here).
 """
@@ -245,7 +245,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mixed", type=int, default=64, help="frames of the mixed-resolution batch (0 = skip)")
-    ap.add_argument("--refine-quads", type=int, default=4096, help="quads of the refinement and pose steps (0 = skip)")
+    ap.add_argument("--refine-quads", type=int, default=4096, help="quads of the refinement, pose and tag-reading steps (0 = skip)")
     ap.add_argument("--serving-seconds", type=float, default=5.0, help="length of the serving run (0 = skip)")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
@@ -468,7 +468,7 @@ def main():
         del detm, gm
 
     # --- corner refinement: forward + hand-written adjoint on 4096 quads
-    refine_line = pose_line = None
+    refine_line = pose_line = decode_line = None
     if args.refine_quads > 0:
         from atag import refine
         g = torch.Generator(device="cpu").manual_seed(3)
@@ -509,6 +509,24 @@ def main():
         pose_line = {"quads": nq, "ms": pms, "poses_per_s": nq / (pms / 1000.0), "max_iterations": 20,
                      "mean_iterations": float(pn["iterations"].mean()),
                      "max_reproj_px": float(pn["reproj_rms"].max()), "degenerate": int((pn["status"] & 2).sum())}
+
+        # --- reading the same quads against a seeded random family of 587
+        # 36-bit codes (the size of tag36h11, whose table is not reproduced)
+        from atag import decode
+        fam = torch.randint(0, 1 << 36, (587,), generator=g, dtype=torch.int64).cuda()
+        grey = torch.from_numpy(host_frames[0]).cuda()
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                dec = decode.decode_quads(grey, quads_c, fam, stream=stream)
+            a.record(stream)
+            for _ in range(args.steps):
+                dec = decode.decode_quads(grey, quads_c, fam, stream=stream)
+            b.record(stream)
+        b.synchronize()
+        dms = a.elapsed_time(b) / args.steps
+        dn = decode.to_numpy(dec)
+        decode_line = {"quads": nq, "family_codes": 587, "ms": dms, "quads_per_s": nq / (dms / 1000.0),
+                       "read": int((dn["status"] == 0).sum())}
 
     # --- serving: 8 cameras (4 x 720p60, 4 x 1080p30), Poisson arrivals
     serving_line = None
@@ -559,6 +577,7 @@ def main():
         "mixed_batch": mixed,
         "refine": refine_line,
         "pose": pose_line,
+        "decode": decode_line,
         "serving": serving_line,
         "tuning": tuning["tuning"] if tuning else None,
         "roofline": roofline,
