@@ -44,7 +44,7 @@ typedef enum atag_status {
 
 /* Device-side status word bits (atag_frame_stats.status). */
 #define ATAG_DEVFLAG_POINT_OVERFLOW 0x1u   /* more boundary points than capacity */
-#define ATAG_DEVFLAG_PAIR_OVERFLOW 0x2u    /* pair hash table full               */
+#define ATAG_DEVFLAG_PAIR_OVERFLOW 0x2u    /* pair hash table (or output) full   */
 #define ATAG_DEVFLAG_CLUSTER_OVERFLOW 0x4u /* more filtered clusters than cap    */
 #define ATAG_DEVFLAG_UF_ITERATION_CAP 0x8u /* union-find merge loop cap hit      */
 #define ATAG_DEVFLAG_QUAD_OVERFLOW 0x10u   /* more quads than output capacity    */
@@ -259,6 +259,92 @@ atag_status atag_process_fitted_quads(const atag_fitted_quad *d_fitted, size_t f
                                       size_t width, size_t height, const atag_config *cfg,
                                       atag_quad_corners *d_quads, size_t quads_capacity,
                                       uint32_t *d_count, atag_stream_t stream);
+
+/* Replaces the oneDPL glue of stages 4-11 (src/main.cpp:467-801): compaction
+ * of the dense boundary planes (point != 0), the sort by pair key, the
+ * per-pair ClusterBounds reduction, ValidBlobFilter, the point-to-cluster
+ * map with calc_theta, the (cluster, slope) sort, compute_initial_linefit
+ * and the segmented prefix sum of the line-fit moments.  Inputs are the
+ * outputs of atag_find_boundaries (4 planes of width*height entries) and the
+ * grey image compute_initial_linefit samples.  Outputs (device arrays the
+ * caller allocates; entries past the counts are left untouched):
+ *   pair_bounds / pair_keys  (optional, NULL to skip) every pair's bounds
+ *                            and key in key order, up to pair_capacity;
+ *   filtered_bounds, filtered_keys (optional), cluster_extents
+ *                            the clusters that pass the filter, up to
+ *                            cluster_capacity (at most 65535: the cluster
+ *                            index is 16 bits, src/main.cpp:641);
+ *   cluster_points, cluster_indices, line_fit_points
+ *                            their points sorted by (cluster, slope), up to
+ *                            point_capacity;
+ *   counts                   n_points (P), n_pairs (C), n_clusters (C_f),
+ *                            n_cluster_points (P_f) and status (ATAG_DEVFLAG_*:
+ *                            a capacity that was too small).
+ * Ties of the reference's unstable sorts are fixed by the packed point.
+ * Scratch memory is the caller's workspace of atag_cluster_workspace_size
+ * bytes.  Stream-ordered; the counts stay on the device. */
+typedef struct atag_cluster_outputs {
+    atag_cluster_bounds *pair_bounds;
+    uint64_t *pair_keys;
+    size_t pair_capacity;
+    atag_cluster_bounds *filtered_bounds;
+    uint64_t *filtered_keys;
+    atag_cluster_extents *cluster_extents;
+    size_t cluster_capacity;
+    atag_cluster_point *cluster_points;
+    uint16_t *cluster_indices;
+    atag_line_fit_point *line_fit_points;
+    size_t point_capacity;
+    atag_frame_stats *counts;
+} atag_cluster_outputs;
+
+atag_status atag_cluster_workspace_size(size_t width, size_t height, size_t cluster_capacity,
+                                        size_t point_capacity, size_t *bytes);
+atag_status atag_cluster(const atag_boundary_point *d_points, const uint64_t *d_blob_labels,
+                         const uint8_t *d_grayscale, size_t width, size_t height, void *d_workspace,
+                         size_t workspace_bytes, const atag_cluster_outputs *outputs, atag_stream_t stream);
+
+/* Replaces stages 13-15 (src/main.cpp:832-907): the corners of
+ * atag_fit_lines whose error is not 0, sorted by (cluster, error
+ * descending; ties by point index), and one PeakExtents {first corner,
+ * count} per cluster that has corners.  d_cluster_extents are the
+ * cluster_count extents atag_cluster wrote (fit_lines writes each
+ * cluster's corners inside its extent).  d_counts (3 words) receives the
+ * corner count K, the PeakExtents count C_p and a status word: corners past
+ * corner_capacity and extents past extents_capacity are dropped and set
+ * ATAG_DEVFLAG_QUAD_OVERFLOW.  Scratch memory is the caller's workspace of
+ * atag_corner_peaks_workspace_size bytes.  Stream-ordered. */
+atag_status atag_corner_peaks_workspace_size(size_t cluster_count, size_t *bytes);
+atag_status atag_corner_peaks(const atag_corner *d_found_corners, const atag_cluster_extents *d_cluster_extents,
+                              size_t cluster_count, void *d_workspace, size_t workspace_bytes,
+                              atag_corner *d_compacted_corners, size_t corner_capacity,
+                              atag_peak_extents *d_peak_extents, size_t extents_capacity, uint32_t *d_counts,
+                              atag_stream_t stream);
+
+/* Host helpers of the reference, evaluated on the host with the device's
+ * roundings (int64 products wrap; hypotf is the double-precision root
+ * rounded to float, as the reference's host library computes it). */
+
+/* get_moment (include/fit_quad.h:39-41, src/fit_quad.cpp:15-35): the moment
+ * of the cyclic range [i0, i1] of one cluster's prefix sums
+ * h_points[0 .. points_size); i0 == i1 gives zero and a count of 0.  The a
+ * and b fields come from the leading operand, as the reference's copy does.
+ * Indices at or past points_size are refused. */
+atag_status atag_get_moment(const atag_line_fit_point *h_points, size_t points_size, size_t i0, size_t i1,
+                            atag_line_fit_point *h_moment, size_t *h_num_in_moment);
+
+/* fit_line (include/fit_quad.h:43-44, src/fit_quad.cpp:37-105): line
+ * parameters (centroid x, y, unit normal x, y), error and mean squared
+ * error of a moment of num_in_moment points; any output may be NULL. */
+atag_status atag_fit_line(const atag_line_fit_point *h_moment, size_t num_in_moment, float *h_line_params,
+                          float *h_err, float *h_mse);
+
+/* compute_initial_linefit (include/line_fit_point.h:50-86): one point's
+ * moment contribution, weighted by 1 + (int)hypotf of the central
+ * difference of the grey image at (rx/2, rx/2) (the reference samples row
+ * rx/2, not ry/2). */
+atag_line_fit_point atag_compute_initial_linefit(atag_cluster_point p, uint32_t width, uint32_t height,
+                                                 const uint8_t *h_greyscaled);
 
 /* ------------------------------------------------------------------ */
 /* Whole-path detector (replaces src/main.cpp:322-1024 stages 1-16 and */

@@ -16,6 +16,7 @@
 
 #include <stdexcept>
 #include <string>
+#include <tuple>
 
 #include "atag.h"
 
@@ -70,6 +71,46 @@ inline atag_status do_indexing(cudaStream_t q, const PeakExtents* extents, size_
                                const ClusterExtents* cluster_extents, FittedQuad* fitted) {
     return atag_do_indexing(extents, extents_count, compacted_corners, points, cluster_extents, fitted,
                             as_stream(q));
+}
+
+// get_moment, include/fit_quad.h:39-41 (host)
+inline std::tuple<LineFitPoint, size_t> get_moment(const LineFitPoint* points, size_t points_size, size_t i0,
+                                                   size_t i1) {
+    LineFitPoint m{};
+    size_t n = 0;
+    if (atag_get_moment(points, points_size, i0, i1, &m, &n) != ATAG_OK)
+        throw std::out_of_range(std::string("get_moment: ") + atag_last_error());
+    return std::make_tuple(m, n);
+}
+
+// fit_line, include/fit_quad.h:43-44 (host)
+inline void fit_line(LineFitPoint moment, size_t num_in_moment, float* line_params, float* err, float* mse) {
+    atag_fit_line(&moment, num_in_moment, line_params, err, mse);
+}
+
+// compute_initial_linefit, include/line_fit_point.h:50-52 (host)
+inline LineFitPoint compute_initial_linefit(ClusterPoint p, uint32_t width, uint32_t height,
+                                            const uint8_t* greyscaled) {
+    return atag_compute_initial_linefit(p, width, height, greyscaled);
+}
+
+// Stages 4-11 of src/main.cpp:467-801 (the oneDPL glue between
+// find_boundaries and fit_lines); counts stay on the device.
+inline atag_status cluster(cudaStream_t q, const BoundaryPoint* points, const uint64_t* blob_labels,
+                           const uint8_t* grayscale, size_t width, size_t height, void* workspace,
+                           size_t workspace_bytes, const atag_cluster_outputs& outputs) {
+    return atag_cluster(points, blob_labels, grayscale, width, height, workspace, workspace_bytes, &outputs,
+                        as_stream(q));
+}
+
+// Stages 13-15 of src/main.cpp:832-907 (between fit_lines and do_indexing).
+inline atag_status corner_peaks(cudaStream_t q, const Corner* found_corners, const ClusterExtents* cluster_extents,
+                                size_t cluster_count, void* workspace, size_t workspace_bytes,
+                                Corner* compacted_corners, size_t corner_capacity, PeakExtents* peak_extents,
+                                size_t extents_capacity, uint32_t* d_counts) {
+    return atag_corner_peaks(found_corners, cluster_extents, cluster_count, workspace, workspace_bytes,
+                             compacted_corners, corner_capacity, peak_extents, extents_capacity, d_counts,
+                             as_stream(q));
 }
 
 // process_fitted_quads, src/main.cpp:1035 (up to, not including, decode_quads)

@@ -7,7 +7,7 @@ import ctypes
 import os
 import re
 
-from .records import Config, Frame, FrameViews, Tuning
+from .records import ClusterOutputs, ClusterPointC, Config, Frame, FrameViews, LineFitPointC, Tuning
 
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_ROOT, "lib", "libatag_gb300.so")
@@ -40,6 +40,13 @@ _SIGNATURES = {
     "atag_fit_lines": (_ST, [_P, _P, _P, _SZ, _P, _P]),
     "atag_do_indexing": (_ST, [_P, _SZ, _P, _P, _P, _P, _P]),
     "atag_process_fitted_quads": (_ST, [_P, _SZ, _SZ, _SZ, ctypes.POINTER(Config), _P, _SZ, _P, _P]),
+    "atag_cluster_workspace_size": (_ST, [_SZ, _SZ, _SZ, _SZ, ctypes.POINTER(_SZ)]),
+    "atag_cluster": (_ST, [_P, _P, _P, _SZ, _SZ, _P, _SZ, ctypes.POINTER(ClusterOutputs), _P]),
+    "atag_corner_peaks_workspace_size": (_ST, [_SZ, ctypes.POINTER(_SZ)]),
+    "atag_corner_peaks": (_ST, [_P, _P, _SZ, _P, _SZ, _P, _SZ, _P, _SZ, _P, _P]),
+    "atag_get_moment": (_ST, [_P, _SZ, _SZ, _SZ, _P, ctypes.POINTER(_SZ)]),
+    "atag_fit_line": (_ST, [_P, _SZ, _P, _P, _P]),
+    "atag_compute_initial_linefit": (LineFitPointC, [ClusterPointC, _U32, _U32, _P]),
     "atag_workspace_size": (_ST, [ctypes.POINTER(Config), _SZ, _SZ, _SZ, _SZ, ctypes.POINTER(_SZ)]),
     "atag_detector_create": (_ST, [ctypes.POINTER(Config), _SZ, _SZ, _SZ, _SZ, _P, _SZ, ctypes.POINTER(_P)]),
     "atag_detector_destroy": (_ST, [_P]),

@@ -72,6 +72,26 @@ DEVFLAG_QUAD_OVERFLOW = 0x10
 DEVFLAG_SORT_OVERFLOW = 0x20
 
 
+class LineFitPointC(ctypes.Structure):
+    """atag_line_fit_point passed by value."""
+    _fields_ = [(n, ctypes.c_int64) for n in ("Mx", "My", "Mxx", "Myy", "Mxy", "W", "a", "b")]
+
+
+class ClusterPointC(ctypes.Structure):
+    """atag_cluster_point passed by value."""
+    _fields_ = [("packed_x", ctypes.c_uint16), ("packed_y", ctypes.c_uint16), ("slope", ctypes.c_float)]
+
+
+class ClusterOutputs(ctypes.Structure):
+    """atag_cluster_outputs: device arrays and capacities atag_cluster writes."""
+    _fields_ = [("pair_bounds", ctypes.c_void_p), ("pair_keys", ctypes.c_void_p), ("pair_capacity", ctypes.c_size_t),
+                ("filtered_bounds", ctypes.c_void_p), ("filtered_keys", ctypes.c_void_p),
+                ("cluster_extents", ctypes.c_void_p), ("cluster_capacity", ctypes.c_size_t),
+                ("cluster_points", ctypes.c_void_p), ("cluster_indices", ctypes.c_void_p),
+                ("line_fit_points", ctypes.c_void_p), ("point_capacity", ctypes.c_size_t),
+                ("counts", ctypes.c_void_p)]
+
+
 class Tuning(ctypes.Structure):
     """atag_tuning: launch shapes of the detector's kernels."""
     _fields_ = [("ccl_tile_rows", ctypes.c_int32), ("boundary_tile_rows", ctypes.c_int32),

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "lib", "obj")
 LIB = os.path.join(HERE, "lib", "libatag_gb300.so")
-SOURCES = ["k_pixels.cu", "k_quads.cu", "k_cluster.cu", "k_refine.cu", "k_pose.cu", "k_decode.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["k_pixels.cu", "k_quads.cu", "k_cluster.cu", "k_refine.cu", "k_pose.cu", "k_decode.cu", "capi.cu", "noalloc.cu", "k_stage_cluster.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",

@@ -262,28 +262,60 @@ __device__ __forceinline__ bool valid_blob(const FilterParams& f, uint32_t count
 // ---------------------------------------------------------------------------
 // Line-fit moments (line_fit_point.h, fit_quad.cpp:15-105)
 // ---------------------------------------------------------------------------
+// Single-precision operations rounded to nearest on both sides: the device
+// spells each one as its _rn intrinsic (never contracted into an FMA), the
+// host build compiles plain operators with -ffp-contract=off.
+__host__ __device__ __forceinline__ float rn_add(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+}
+__host__ __device__ __forceinline__ float rn_sub(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+}
+__host__ __device__ __forceinline__ float rn_mul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
+__host__ __device__ __forceinline__ float rn_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+}
+
 struct Moment {
     long long Mx, My, Mxx, Myy, Mxy, W;
 };
 
-__device__ __forceinline__ Moment load_moment(const atag_line_fit_point* p) {
+__host__ __device__ __forceinline__ Moment load_moment(const atag_line_fit_point* p) {
     const longlong2* q = reinterpret_cast<const longlong2*>(p);
     longlong2 a = q[0], b = q[1], c = q[2];
     return Moment{a.x, a.y, b.x, b.y, c.x, c.y};
 }
-__device__ __forceinline__ void store_moment(atag_line_fit_point* p, const Moment& m) {
+__host__ __device__ __forceinline__ void store_moment(atag_line_fit_point* p, const Moment& m) {
     longlong2* q = reinterpret_cast<longlong2*>(p);
     q[0] = make_longlong2(m.Mx, m.My);
     q[1] = make_longlong2(m.Mxx, m.Myy);
     q[2] = make_longlong2(m.Mxy, m.W);
     q[3] = make_longlong2(0, 0);
 }
-__device__ __forceinline__ Moment m_add(Moment a, const Moment& b) {
+__host__ __device__ __forceinline__ Moment m_add(Moment a, const Moment& b) {
     a.Mx = wadd(a.Mx, b.Mx); a.My = wadd(a.My, b.My); a.Mxx = wadd(a.Mxx, b.Mxx);
     a.Myy = wadd(a.Myy, b.Myy); a.Mxy = wadd(a.Mxy, b.Mxy); a.W = wadd(a.W, b.W);
     return a;
 }
-__device__ __forceinline__ Moment m_sub(Moment a, const Moment& b) {
+__host__ __device__ __forceinline__ Moment m_sub(Moment a, const Moment& b) {
     a.Mx = wsub(a.Mx, b.Mx); a.My = wsub(a.My, b.My); a.Mxx = wsub(a.Mxx, b.Mxx);
     a.Myy = wsub(a.Myy, b.Myy); a.Mxy = wsub(a.Mxy, b.Mxy); a.W = wsub(a.W, b.W);
     return a;
@@ -291,24 +323,35 @@ __device__ __forceinline__ Moment m_sub(Moment a, const Moment& b) {
 
 // Integer floor(sqrt(v)) for v < 2^17: equals (int64)hypotf(gx, gy) for the
 // central differences of a u8 image (line_fit_point.h:70-75).
-__device__ __forceinline__ uint32_t isqrt_small(uint32_t v) {
+__host__ __device__ __forceinline__ uint32_t isqrt_small(uint32_t v) {
+#ifdef __CUDA_ARCH__
     uint32_t r = (uint32_t)__fsqrt_rn((float)v);
+#else
+    uint32_t r = (uint32_t)sqrtf((float)v);
+#endif
     while (r * r > v) r--;
     while ((r + 1) * (r + 1) <= v) r++;
     return r;
 }
 
 // compute_initial_linefit, line_fit_point.h:50-86 (weight row rx/2, sic).
-__device__ __forceinline__ Moment initial_linefit(uint32_t packed, uint32_t width, uint32_t height,
-                                                  const uint8_t* __restrict__ grey) {
+__host__ __device__ __forceinline__ uint32_t grey_at(const uint8_t* __restrict__ grey, size_t i) {
+#ifdef __CUDA_ARCH__
+    return __ldg(grey + i);
+#else
+    return grey[i];
+#endif
+}
+__host__ __device__ __forceinline__ Moment initial_linefit(uint32_t packed, uint32_t width, uint32_t height,
+                                                           const uint8_t* __restrict__ grey) {
     long long rx = (long long)bp_xd(packed) + 1;
     long long ry = (long long)bp_yd(packed) + 1;
     uint32_t x = (uint32_t)(rx / 2);
     uint32_t y = (uint32_t)(rx / 2);
     long long W = 1;
     if (x > 0 && x + 1 < width && y > 0 && y + 1 < height) {
-        int gx = (int)__ldg(grey + (size_t)y * width + x + 1) - (int)__ldg(grey + (size_t)y * width + x - 1);
-        int gy = (int)__ldg(grey + (size_t)(y + 1) * width + x) - (int)__ldg(grey + (size_t)(y - 1) * width + x);
+        int gx = (int)grey_at(grey, (size_t)y * width + x + 1) - (int)grey_at(grey, (size_t)y * width + x - 1);
+        int gy = (int)grey_at(grey, (size_t)(y + 1) * width + x) - (int)grey_at(grey, (size_t)(y - 1) * width + x);
         W += (long long)isqrt_small((uint32_t)(gx * gx + gy * gy));
     }
     return Moment{W * rx, W * ry, W * rx * rx, W * ry * ry, W * rx * ry, W};
@@ -336,7 +379,7 @@ __device__ __forceinline__ Moment moment_of(unsigned long long v) {
 }
 
 // get_moment, fit_quad.cpp:15-35 over a prefix-sum array of one cluster.
-__device__ __forceinline__ Moment get_moment(const atag_line_fit_point* points, unsigned long long n,
+__host__ __device__ __forceinline__ Moment get_moment(const atag_line_fit_point* points, unsigned long long n,
                                              unsigned long long i0, unsigned long long i1,
                                              unsigned long long* total) {
     Moment r{0, 0, 0, 0, 0, 0};
@@ -355,7 +398,7 @@ __device__ __forceinline__ Moment get_moment(const atag_line_fit_point* points, 
 }
 
 // fit_line, fit_quad.cpp:37-105.
-__device__ __forceinline__ void fit_line(const Moment& m, unsigned long long num_in_moment, float* lp,
+__host__ __device__ __forceinline__ void fit_line(const Moment& m, unsigned long long num_in_moment, float* lp,
                                          float* err, float* mse) {
     long long Csxx = wsub(wmul(m.Mxx, m.W), wmul(m.Mx, m.Mx));
     long long Csxy = wsub(wmul(m.Mxy, m.W), wmul(m.Mx, m.My));
@@ -363,30 +406,30 @@ __device__ __forceinline__ void fit_line(const Moment& m, unsigned long long num
     long long cf = wmul(wmul(m.W, m.W), 4);
     const float dxy = i64_to_f32_rn(wsub(Csxx, Csyy)), cxy2 = i64_to_f32_rn(wmul(2, Csxy));
     float sdist = hypot_f(dxy, cxy2);
-    float num = __fsub_rn(i64_to_f32_rn(wadd(Csxx, Csyy)), sdist);
-    float eig = __fdiv_rn(num, i64_to_f32_rn(wmul(cf, 2)));
+    float num = rn_sub(i64_to_f32_rn(wadd(Csxx, Csyy)), sdist);
+    float eig = rn_div(num, i64_to_f32_rn(wmul(cf, 2)));
     if (lp) {
-        float nx1 = __fsub_rn(dxy, sdist);
+        float nx1 = rn_sub(dxy, sdist);
         float ny1 = cxy2;
         float nx2 = ny1;
-        float ny2 = __fsub_rn(i64_to_f32_rn(wsub(Csyy, Csxx)), sdist);
-        float M1 = __fadd_rn(__fmul_rn(nx1, nx1), __fmul_rn(ny1, ny1));
-        float M2 = __fadd_rn(__fmul_rn(nx2, nx2), __fmul_rn(ny2, ny2));
+        float ny2 = rn_sub(i64_to_f32_rn(wsub(Csyy, Csxx)), sdist);
+        float M1 = rn_add(rn_mul(nx1, nx1), rn_mul(ny1, ny1));
+        float M2 = rn_add(rn_mul(nx2, nx2), rn_mul(ny2, ny2));
         float nx, ny;
         if (M1 > M2) { nx = nx1; ny = ny1; } else { nx = nx2; ny = ny2; }
         float w2 = i64_to_f32_rn(wmul(m.W, 2));
-        lp[0] = __fdiv_rn(i64_to_f32_rn(m.Mx), w2);
-        lp[1] = __fdiv_rn(i64_to_f32_rn(m.My), w2);
+        lp[0] = rn_div(i64_to_f32_rn(m.Mx), w2);
+        lp[1] = rn_div(i64_to_f32_rn(m.My), w2);
         float length = hypot_f(nx, ny);
         if (fabsf(length) < 0x1.19799ap-40f) {  // (double)|length| < 1e-12, in float
             lp[2] = 0.0f;
             lp[3] = 0.0f;
         } else {
-            lp[2] = __fdiv_rn(nx, length);
-            lp[3] = __fdiv_rn(ny, length);
+            lp[2] = rn_div(nx, length);
+            lp[3] = rn_div(ny, length);
         }
     }
-    if (err) *err = __fmul_rn(u64_to_f32_rn(num_in_moment), eig);
+    if (err) *err = rn_mul(u64_to_f32_rn(num_in_moment), eig);
     if (mse) *mse = eig;
 }
 

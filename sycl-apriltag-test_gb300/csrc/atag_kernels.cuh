@@ -67,6 +67,11 @@ struct FrameDesc {
     // DEAD_PAIRS keys (EMPTY = ~0) of pairs whose running point count is
     // already above the cluster size limit; null when not tracked
     unsigned long long* dead_pairs;
+    // optional (stage entry point): every pair's ClusterBounds and key in
+    // key order, up to pair_out_cap entries; null in the fused path
+    atag_cluster_bounds* pair_bounds_out;
+    unsigned long long* pair_keys_out;
+    uint32_t pair_out_cap;
     // 1: write the reference's complete segmentation arrays (every parent
     // compressed to its root, block information words at odd rows, zero
     // sizes away from roots).  0 (fused batches): only what later stages
@@ -183,5 +188,25 @@ __global__ void k_batch_offsets(const __grid_constant__ FrameSet fs, uint32_t n_
 __global__ void k_index_quads(const __grid_constant__ FrameSet fs, const uint32_t* work_offsets, uint32_t n_frames,
                               PipelineParams p);
 __global__ void k_compact_quads(const __grid_constant__ FrameSet fs);
+
+// k_stage_cluster.cu (stage entry points over the dense boundary planes)
+__global__ void k_planes_pairs(const __grid_constant__ FrameSet fs, const uint32_t* __restrict__ points,
+                               const unsigned long long* __restrict__ keys, uint32_t n);
+__global__ void k_planes_scatter(const __grid_constant__ FrameSet fs, const uint32_t* __restrict__ points,
+                                 const unsigned long long* __restrict__ keys, uint32_t n);
+__global__ void k_stage_cluster_out(const __grid_constant__ FrameSet fs, uint16_t* cluster_indices,
+                                    unsigned long long* cluster_keys_out);
+// corner peaks (stages 13-15): per-cluster counts, offsets and sorted corners
+constexpr uint32_t PK_SORT_CAP = 16384;  // corners of one cluster (at most half its points)
+constexpr uint32_t PK_SMEM = PK_SORT_CAP * 8;
+__global__ void k_peaks_count(const atag_corner* __restrict__ found, const atag_cluster_extents* __restrict__ ext,
+                              uint32_t n_clusters, uint32_t* __restrict__ counts);
+__global__ void k_peaks_offsets(const uint32_t* __restrict__ counts, uint32_t n_clusters,
+                                uint32_t* __restrict__ offsets, atag_peak_extents* __restrict__ peak_extents,
+                                uint32_t extents_cap, uint32_t corner_cap, uint32_t* __restrict__ d_counts);
+__global__ void k_peaks_sort(const atag_corner* __restrict__ found, const atag_cluster_extents* __restrict__ ext,
+                             uint32_t n_clusters, const uint32_t* __restrict__ counts,
+                             const uint32_t* __restrict__ offsets, atag_corner* __restrict__ out,
+                             uint32_t corner_cap, uint32_t* __restrict__ d_counts);
 
 }  // namespace atag

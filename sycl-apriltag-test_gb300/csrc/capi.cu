@@ -70,6 +70,7 @@ atag_status ensure_device(DeviceInfo** out) {
         if (e != cudaSuccess) return fail(ATAG_ERR_NO_DEVICE, "kernels do not load: %s", cudaGetErrorString(e));
         CK(cudaFuncSetAttribute(k_cluster_sort_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF_LARGE_SMEM));
         CK(cudaFuncSetAttribute(k_cluster_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF_SMALL_SMEM));
+        CK(cudaFuncSetAttribute(k_peaks_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)PK_SMEM));
         d.num_sms = prop.multiProcessorCount;
         d.smem_optin = prop.sharedMemPerBlockOptin;
         d.device = dev;
@@ -200,6 +201,54 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, bool ow
 constexpr int RING = 16;
 constexpr size_t WORK_LISTS = 5;  // batch-wide work lists of the per-cluster kernels
 constexpr int MAX_LANES = 4;      // sub-batches of one call that run concurrently
+
+// Workspace of atag_cluster: the pair table and the cluster scratch of one
+// frame (the outputs are the caller's arrays), plus the counters, a stats
+// record for callers that pass none and the work offsets of the sorts.
+struct StageClusterLayout {
+    size_t bytes;
+    FrameDesc d;
+    atag_frame_stats* stats;
+    uint32_t* work;  // small/large offsets (2 words each), then 2 queue cursors
+};
+StageClusterLayout layout_stage_cluster(char* base, uint32_t w, uint32_t h, uint32_t cluster_cap, uint32_t cpoint_cap) {
+    StageClusterLayout L;
+    const FrameCaps c = caps_for((size_t)w * h);
+    size_t off = 0;
+    auto take = [&](size_t bytes) -> char* {
+        char* p = base ? base + off : nullptr;
+        off += al(bytes);
+        return p;
+    };
+    FrameDesc f = blank();
+    f.width = w;
+    f.height = h;
+    f.factor = 1;
+    f.pair_cap = c.pair_cap;
+    f.pair_keys = (unsigned long long*)take(8ull * c.pair_cap);
+    f.pair_bbox = (uint4*)take(16ull * c.pair_cap);
+    f.pair_gsum = (int2*)take(8ull * c.pair_cap);
+    f.pair_pxgx = (unsigned long long*)take(8ull * c.pair_cap);
+    f.pair_count = (uint32_t*)take(4ull * c.pair_cap);
+    f.pair_cluster = (uint32_t*)take(4ull * c.pair_cap);
+    f.cluster_cap = cluster_cap;
+    f.cluster_keys = (unsigned long long*)take(8ull * ((size_t)cluster_cap + c.pair_cap));
+    f.cluster_center = (float2*)take(8ull * cluster_cap);
+    f.cluster_cursor = (uint32_t*)take(4ull * cluster_cap);
+    f.peak_count = (uint32_t*)take(4ull * cluster_cap);
+    f.cluster_work = (uint32_t*)take(4ull * cluster_cap);
+    f.cluster_runs = (uint32_t*)take(4ull * cluster_cap);
+    f.cpoint_cap = cpoint_cap;
+    f.sortbuf = (unsigned long long*)take(8ull * cpoint_cap);
+    f.errbuf = (float*)take(8ull * cpoint_cap);
+    f.counters = (uint32_t*)take(4ull * CNT_COUNT);
+    f.stage_outputs = 1;
+    L.stats = (atag_frame_stats*)take(sizeof(atag_frame_stats));
+    L.work = (uint32_t*)take(4ull * 6);
+    L.d = f;
+    L.bytes = off;
+    return L;
+}
 
 }  // namespace
 
@@ -465,6 +514,168 @@ atag_status atag_process_fitted_quads(const atag_fitted_quad* fitted, size_t cou
     k_process_quads<<<1, 256, 0, (cudaStream_t)stream>>>(fitted, count, make_params(c), quads, cap, d_count);
     LAUNCHED();
     return ATAG_OK;
+}
+
+// ------------------------------------------------------------------ stage glue
+
+static bool stage_cluster_caps(size_t w, size_t h, size_t cluster_capacity, size_t point_capacity,
+                               uint32_t* ccap, uint32_t* pcap) {
+    if (!valid_dims(w, h) || cluster_capacity == 0 || point_capacity == 0) return false;
+    *ccap = (uint32_t)std::min<size_t>(cluster_capacity, 65535);  // 16-bit cluster index
+    *pcap = (uint32_t)std::min<size_t>(point_capacity, 4 * w * h);  // at most 4 points per pixel
+    return true;
+}
+
+atag_status atag_cluster_workspace_size(size_t w, size_t h, size_t cluster_capacity, size_t point_capacity,
+                                        size_t* bytes) {
+    uint32_t cc, pc;
+    if (!bytes || !stage_cluster_caps(w, h, cluster_capacity, point_capacity, &cc, &pc))
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "cluster_workspace_size: bad size or capacity");
+    *bytes = layout_stage_cluster(nullptr, (uint32_t)w, (uint32_t)h, cc, pc).bytes + ALIGN;
+    return ATAG_OK;
+}
+
+atag_status atag_cluster(const atag_boundary_point* points, const uint64_t* keys, const uint8_t* grey, size_t w,
+                         size_t h, void* ws, size_t ws_bytes, const atag_cluster_outputs* o, atag_stream_t stream) {
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    uint32_t cc, pc;
+    if (!o || !stage_cluster_caps(w, h, o->cluster_capacity, o->point_capacity, &cc, &pc))
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "cluster: bad size or capacity");
+    if (!points || !keys || !grey || !ws || !o->filtered_bounds || !o->cluster_extents || !o->cluster_points ||
+        !o->cluster_indices || !o->line_fit_points)
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "cluster: null pointer");
+    if ((o->pair_bounds || o->pair_keys) && o->pair_capacity == 0)
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "cluster: pair outputs without a pair capacity");
+    char* base = (char*)(((uintptr_t)ws + ALIGN - 1) / ALIGN * ALIGN);
+    StageClusterLayout L = layout_stage_cluster(base, (uint32_t)w, (uint32_t)h, cc, pc);
+    if ((size_t)(base - (char*)ws) + L.bytes > ws_bytes)
+        return fail(ATAG_ERR_OUT_OF_MEMORY, "cluster: workspace of %zu bytes is too small", ws_bytes);
+    FrameDesc d = L.d;
+    d.grey = const_cast<uint8_t*>(grey);
+    d.cluster_bounds = o->filtered_bounds;
+    d.cluster_extents = o->cluster_extents;
+    d.cluster_points = o->cluster_points;
+    d.line_fit = o->line_fit_points;
+    d.stats = o->counts ? o->counts : L.stats;
+    d.pair_bounds_out = o->pair_bounds;
+    d.pair_keys_out = (unsigned long long*)o->pair_keys;
+    d.pair_out_cap = (uint32_t)std::min<size_t>(o->pair_capacity, 0xFFFFFFFFu);
+    const FrameSet fs = single(d);
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t n = (uint32_t)(4 * w * h);
+    const int sms = dev->num_sms;
+    uint32_t* off_small = L.work;
+    uint32_t* off_large = L.work + 2;
+    uint32_t* wc = L.work + 4;
+    atag_config c;
+    atag_config_default(&c);
+    const PipelineParams p = make_params(c);
+    k_reset_frames<<<grid2(cdiv(d.pair_cap, 256), 1), 256, 0, s>>>(fs);
+    LAUNCHED();
+    k_planes_pairs<<<(unsigned)std::min<size_t>(cdiv(n, 256), (size_t)sms * 8), 256, 0, s>>>(
+        fs, reinterpret_cast<const uint32_t*>(points), reinterpret_cast<const unsigned long long*>(keys), n);
+    LAUNCHED();
+    k_pairs_finalize<<<1, 1024, 0, s>>>(fs, p, CF_SMALL_CAP);
+    LAUNCHED();
+    {
+        BatchOffsets bo{{CNT_SMALL, CNT_LARGE, 0, 0}, {off_small, off_large, nullptr, nullptr}, wc};
+        k_batch_offsets<<<1, 1024, 0, s>>>(fs, 1, bo);
+    }
+    LAUNCHED();
+    k_planes_scatter<<<(unsigned)std::min<size_t>(cdiv(n, 256), (size_t)sms * 8), 256, 0, s>>>(
+        fs, reinterpret_cast<const uint32_t*>(points), reinterpret_cast<const unsigned long long*>(keys), n);
+    LAUNCHED();
+    k_cluster_sort_large<<<std::max(1, sms / 2), CF_LARGE_THREADS, CF_LARGE_SMEM, s>>>(fs, off_large, 1, wc + 1);
+    LAUNCHED();
+    k_cluster_sort_small<<<sms * 8, CF_SMALL_THREADS, CF_SMALL_SMEM, s>>>(fs, off_small, 1, wc, CF_SMALL_CAP);
+    LAUNCHED();
+    k_stage_cluster_out<<<sms * 4, 256, 0, s>>>(fs, o->cluster_indices, (unsigned long long*)o->filtered_keys);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+atag_status atag_corner_peaks_workspace_size(size_t cluster_count, size_t* bytes) {
+    if (!bytes) return fail(ATAG_ERR_INVALID_ARGUMENT, "corner_peaks_workspace_size: null pointer");
+    *bytes = al(8 * std::max<size_t>(cluster_count, 1)) + ALIGN;
+    return ATAG_OK;
+}
+
+atag_status atag_corner_peaks(const atag_corner* found, const atag_cluster_extents* extents, size_t n_clusters,
+                              void* ws, size_t ws_bytes, atag_corner* out, size_t corner_cap,
+                              atag_peak_extents* peak_extents, size_t extents_cap, uint32_t* d_counts,
+                              atag_stream_t stream) {
+    DeviceInfo* dev;
+    atag_status st = ensure_device(&dev);
+    if (st) return st;
+    if (!d_counts) return fail(ATAG_ERR_INVALID_ARGUMENT, "corner_peaks: null counts");
+    if (n_clusters > 65535) return fail(ATAG_ERR_INVALID_ARGUMENT, "corner_peaks: more than 65535 clusters");
+    if (n_clusters && (!found || !extents || !ws || (corner_cap && !out) || (extents_cap && !peak_extents)))
+        return fail(ATAG_ERR_INVALID_ARGUMENT, "corner_peaks: null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (n_clusters == 0) {
+        CK(cudaMemsetAsync(d_counts, 0, 3 * sizeof(uint32_t), s));
+        return ATAG_OK;
+    }
+    uint32_t* counts = (uint32_t*)(((uintptr_t)ws + ALIGN - 1) / ALIGN * ALIGN);
+    uint32_t* offsets = counts + n_clusters;
+    if ((size_t)((char*)(offsets + n_clusters) - (char*)ws) > ws_bytes)
+        return fail(ATAG_ERR_OUT_OF_MEMORY, "corner_peaks: workspace of %zu bytes is too small", ws_bytes);
+    const uint32_t nc = (uint32_t)n_clusters;
+    const uint32_t ccap = (uint32_t)std::min<size_t>(corner_cap, 0xFFFFFFFFu);
+    const uint32_t ecap = (uint32_t)std::min<size_t>(extents_cap, 0xFFFFFFFFu);
+    const int sms = dev->num_sms;
+    k_peaks_count<<<(unsigned)std::min<size_t>(cdiv(nc, 8), (size_t)sms * 8), 256, 0, s>>>(found, extents, nc, counts);
+    LAUNCHED();
+    k_peaks_offsets<<<1, 1024, 0, s>>>(counts, nc, offsets, peak_extents, ecap, ccap, d_counts);
+    LAUNCHED();
+    k_peaks_sort<<<(unsigned)std::min<size_t>(nc, (size_t)sms * 2), 256, PK_SMEM, s>>>(found, extents, nc, counts,
+                                                                                        offsets, out, ccap, d_counts);
+    LAUNCHED();
+    return ATAG_OK;
+}
+
+// ------------------------------------------------------------------ host helpers
+
+atag_status atag_get_moment(const atag_line_fit_point* points, size_t n, size_t i0, size_t i1,
+                            atag_line_fit_point* out, size_t* num) {
+    if (!points || !out || !num) return fail(ATAG_ERR_INVALID_ARGUMENT, "get_moment: null pointer");
+    if (i0 >= n || i1 >= n) return fail(ATAG_ERR_INVALID_ARGUMENT, "get_moment: range [%zu, %zu] outside %zu points", i0, i1, n);
+    unsigned long long cnt = 0;
+    const Moment m = get_moment(points, n, i0, i1, &cnt);
+    atag_line_fit_point r;
+    memset(&r, 0, sizeof r);
+    store_moment(&r, m);
+    // the reference copies the leading operand, a and b included
+    const atag_line_fit_point* lead = i0 < i1 ? &points[i1] : (i1 < i0 ? &points[n - 1] : nullptr);
+    if (lead) {
+        r.a = lead->a;
+        r.b = lead->b;
+    }
+    *out = r;
+    *num = (size_t)cnt;
+    return ATAG_OK;
+}
+
+atag_status atag_fit_line(const atag_line_fit_point* moment, size_t num, float* lp, float* err, float* mse) {
+    if (!moment) return fail(ATAG_ERR_INVALID_ARGUMENT, "fit_line: null moment");
+    fit_line(load_moment(moment), (unsigned long long)num, lp, err, mse);
+    return ATAG_OK;
+}
+
+atag_line_fit_point atag_compute_initial_linefit(atag_cluster_point p, uint32_t width, uint32_t height,
+                                                 const uint8_t* grey) {
+    atag_line_fit_point r;
+    memset(&r, 0, sizeof r);
+    const uint32_t packed = (uint32_t)p.packed_x | ((uint32_t)p.packed_y << 16);
+    if (grey) {
+        store_moment(&r, initial_linefit(packed, width, height, grey));
+    } else {
+        // no image: every weight is 1, as outside the image
+        store_moment(&r, initial_linefit(packed, 0, 0, nullptr));
+    }
+    return r;
 }
 
 // ------------------------------------------------------------------ detector

@@ -26,15 +26,10 @@
 //   5. k_peaks_scan / k_index_quads / k_compact_quads: peak extents,
 //      do_indexing and the corner intersection, quads in reference order.
 #include "atag_kernels.cuh"
+#include "atag_pairs.cuh"
 #include "atag_quads.cuh"
 
 namespace atag {
-
-constexpr unsigned long long EMPTY_KEY = ~0ull;
-
-__device__ __forceinline__ uint32_t hash_key(unsigned long long k) {
-    return (uint32_t)((k * 0x9E3779B97F4A7C15ull) >> 32);
-}
 
 // ---------------------------------------------------------------------------
 // reset
@@ -84,41 +79,6 @@ __device__ __forceinline__ int local_insert(PairTableSmem& T, unsigned long long
     }
     return -1;
 }
-__device__ __forceinline__ uint32_t global_insert(const FrameDesc& F, unsigned long long key) {
-    uint32_t mask = F.pair_cap - 1, h = hash_key(key) & mask;
-    for (uint32_t p = 0; p < F.pair_cap; p++) {
-        unsigned long long k = atomicCAS(&F.pair_keys[h], EMPTY_KEY, key);
-        if (k == EMPTY_KEY || k == key) return h;
-        h = (h + 1) & mask;
-    }
-    return INVALID;
-}
-__device__ __forceinline__ uint32_t global_lookup(const FrameDesc& F, unsigned long long key) {
-    uint32_t mask = F.pair_cap - 1, h = hash_key(key) & mask;
-    for (uint32_t p = 0; p < F.pair_cap; p++) {
-        unsigned long long k = F.pair_keys[h];
-        if (k == key) return h;
-        if (k == EMPTY_KEY) return INVALID;
-        h = (h + 1) & mask;
-    }
-    return INVALID;
-}
-__device__ __forceinline__ uint32_t global_flush(const FrameDesc& F, uint32_t gs, uint32_t cnt, uint32_t xmin,
-                                                 uint32_t xmax, uint32_t ymin, uint32_t ymax, int gx, int gy,
-                                                 unsigned long long pxgx) {
-    uint32_t old = atomicAdd(&F.pair_count[gs], cnt);
-    uint32_t* bb = reinterpret_cast<uint32_t*>(&F.pair_bbox[gs]);
-    atomicMin(bb + 0, xmin);
-    atomicMax(bb + 1, xmax);
-    atomicMin(bb + 2, ymin);
-    atomicMax(bb + 3, ymax);
-    int* gsum = reinterpret_cast<int*>(&F.pair_gsum[gs]);
-    if (gx) atomicAdd(gsum + 0, gx);
-    if (gy) atomicAdd(gsum + 1, gy);
-    if (pxgx) atomicAdd(&F.pair_pxgx[gs], pxgx);
-    return old;
-}
-
 // A staged point: CTA table slot (8 bits), tile-relative x (6) and y (4),
 // neighbour test (2) and colour direction (1).
 constexpr uint32_t STAGE_DIRECT = 1u << 21; // point already accounted for in global memory
@@ -441,6 +401,22 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
         }
         uint32_t tot_cnt, tot_keep, tot_fcnt, tot_small, tot_large, tot_fit, tot_runs;
         uint32_t start = carry_start + block_exclusive_scan_u32(cnt, red, &tot_cnt);
+        if (c < C && F.pair_bounds_out) {
+            // every pair's bounds in key order (stages 5-6 of the reference)
+            if (c < F.pair_out_cap) {
+                atag_cluster_bounds b;
+                b.x_min = (uint16_t)bb.x; b.x_max = (uint16_t)bb.y;
+                b.y_min = (uint16_t)bb.z; b.y_max = (uint16_t)bb.w;
+                b.gx_sum = gs.x; b.gy_sum = gs.y;
+                b.pxgx_pygy_sum = pxgx;
+                b.start = start;
+                b.count = cnt;
+                F.pair_bounds_out[c] = b;
+                if (F.pair_keys_out) F.pair_keys_out[c] = keys[c];
+            } else {
+                atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
+            }
+        }
         uint32_t cid = carry_cluster + block_exclusive_scan_u32(keep ? 1u : 0u, red, &tot_keep);
         uint32_t fstart = carry_fstart + block_exclusive_scan_u32(keep ? cnt : 0u, red, &tot_fcnt);
         const bool fits = keep && cid < F.cluster_cap && (unsigned long long)fstart + cnt <= F.cpoint_cap;

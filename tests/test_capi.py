@@ -70,6 +70,16 @@ def test_workspace_size_validates_arguments():
     assert m.value > n.value
 
 
+def test_stage_workspace_sizes_validate_arguments():
+    L = lib.load()
+    n = ctypes.c_size_t()
+    assert L.atag_cluster_workspace_size(1920, 1080, 65535, 1 << 20, ctypes.byref(n)) == 0
+    assert n.value > 16 * (1 << 20)
+    assert L.atag_cluster_workspace_size(1922, 1080, 65535, 1 << 20, ctypes.byref(n)) == 1
+    assert L.atag_cluster_workspace_size(1920, 1080, 0, 1 << 20, ctypes.byref(n)) == 1
+    assert L.atag_corner_peaks_workspace_size(100, ctypes.byref(n)) == 0 and n.value >= 800
+
+
 def test_calls_without_device_return_status(monkeypatch):
     import torch
     if torch.cuda.is_available():
@@ -84,6 +94,8 @@ def test_calls_without_device_return_status(monkeypatch):
     assert st == 5
     assert L.atag_refine_forward(None, 64, 64, None, 1, None, None, None, None) == 5
     assert L.atag_decode_quads(None, 64, 64, 64, None, 32, 1, None, 0, 6, 2, 10.0, None, None) == 5
+    assert L.atag_cluster(None, None, None, 64, 64, None, 0, None, None) == 5
+    assert L.atag_corner_peaks(None, None, 1, None, 0, None, 0, None, 0, None, None) == 5
 
 
 def test_cpp_header_compiles_against_the_c_abi(tmp_path):
