@@ -381,7 +381,13 @@ atag_status atag_detector_destroy(atag_detector *det);
  * frame to d_quads + f*quads_capacity and the frame's counters to
  * d_stats[f].  Stream-ordered, no host synchronisation: every stage sizes
  * its grid from upper bounds and reads its counts on the device, so the
- * call can be captured in a CUDA graph. */
+ * call can be captured in a CUDA graph.  A captured call keeps its own copy
+ * of the frame table, so its graph detects the captured frames on every
+ * replay, whatever eager calls the detector makes in between; up to 16
+ * different captured tables per detector (identical ones share a copy),
+ * after which a capture fails with ATAG_ERR_CAPACITY until
+ * atag_detector_release_captures.  Replays and eager calls share the
+ * detector's workspace: they must not overlap on the GPU. */
 atag_status atag_detect_batch(atag_detector *det, const atag_frame *h_frames, size_t n_frames,
                               atag_quad_corners *d_quads, size_t quads_capacity,
                               atag_frame_stats *d_stats, atag_stream_t stream);
@@ -427,6 +433,10 @@ typedef struct atag_frame_views {
     const uint32_t *peak_clusters;              /* n_peak_clusters: rank -> cluster */
     const atag_peak_extents *peak_extents;      /* n_peak_clusters                  */
     const atag_fitted_quad *fitted;             /* n_peak_clusters (by rank)        */
+    uint32_t point_capacity;                    /* entries of pair_points           */
+    uint32_t cluster_capacity;                  /* filtered clusters                */
+    uint32_t cluster_point_capacity;            /* points of filtered clusters      */
+    uint32_t reserved_;
 } atag_frame_views;
 
 /* Selects the CUDA device this library launches on for the calling host
@@ -434,6 +444,30 @@ typedef struct atag_frame_views {
 atag_status atag_use_device(int ordinal);
 
 atag_status atag_detector_views(const atag_detector *det, size_t frame, atag_frame_views *out);
+
+/* Per-frame capacities and iteration caps below the ones the detector sizes
+ * for itself, for callers that bound a frame's work and for exercising the
+ * device status flags.  0 keeps a field's default; values above the default
+ * are clipped to it, so a limit never needs more workspace.  Work past a
+ * capacity is dropped and flagged in atag_frame_stats.status; nothing is
+ * written past it.  Applies to later detect calls. */
+typedef struct atag_limits {
+    uint32_t point_capacity;         /* listed boundary points (ATAG_DEVFLAG_POINT_OVERFLOW)        */
+    uint32_t pair_capacity;          /* pair table slots, rounded down to a power of two
+                                        (ATAG_DEVFLAG_PAIR_OVERFLOW)                              */
+    uint32_t cluster_capacity;       /* filtered clusters (ATAG_DEVFLAG_CLUSTER_OVERFLOW)           */
+    uint32_t cluster_point_capacity; /* points of filtered clusters (ATAG_DEVFLAG_CLUSTER_OVERFLOW) */
+    uint32_t uf_iteration_cap;       /* parents one frame-wide union-find walk follows and retries of
+                                        one union (ATAG_DEVFLAG_UF_ITERATION_CAP); the default is
+                                        the bound the CCL tile count gives for a w x h frame,
+                                        2 + 160 ceil(w / 64) ceil(h / 16)                       */
+    uint32_t reserved[3];
+} atag_limits;
+atag_status atag_detector_set_limits(atag_detector *det, const atag_limits *limits);
+
+/* Frees the frame-table copies held for captured calls; call it once every
+ * graph captured from this detector has been destroyed. */
+atag_status atag_detector_release_captures(atag_detector *det);
 
 /* Intermediates of later detect calls.  By default a detector writes only
  * what its own later stages read: labels in full, parents at even rows and

@@ -58,6 +58,17 @@ class Detector:
         lib.check(self.L.atag_detector_keep_intermediates(self.handle, 1 if keep else 0),
                   "atag_detector_keep_intermediates")
 
+    def set_limits(self, **fields):
+        """Per-frame capacities and the union-find iteration cap of later
+        calls (atag_limits; 0 or absent = the detector's own sizing):
+        point_capacity, pair_capacity, cluster_capacity,
+        cluster_point_capacity, uf_iteration_cap."""
+        from .records import Limits
+        lim = Limits()
+        for k, v in fields.items():
+            setattr(lim, k, int(v))
+        lib.check(self.L.atag_detector_set_limits(self.handle, ctypes.byref(lim)), "atag_detector_set_limits")
+
     def close(self):
         if self.handle:
             self.L.atag_detector_destroy(self.handle)
@@ -95,12 +106,19 @@ class Detector:
     def stats(self) -> np.ndarray:
         return self.d_stats[: self._n * FRAME_STATS.itemsize].cpu().numpy().view(FRAME_STATS)
 
-    def results(self):
-        """(list of QUAD_CORNERS arrays, stats array) of the last enqueue."""
-        st = self.stats()
-        q = self.d_quads[: self._n * self.quad_capacity * QUAD_CORNERS.itemsize].cpu().numpy().view(QUAD_CORNERS)
-        q = q.reshape(self._n, self.quad_capacity)
-        return [q[i, : int(st[i]["n_quads"])].copy() for i in range(self._n)], st
+    def results(self, n_frames: int = None):
+        """(list of QUAD_CORNERS arrays, stats array) of the last enqueue, or
+        of the first n_frames output slots (e.g. after a graph replay)."""
+        n = self._n if n_frames is None else n_frames
+        st = self.d_stats[: n * FRAME_STATS.itemsize].cpu().numpy().view(FRAME_STATS)
+        q = self.d_quads[: n * self.quad_capacity * QUAD_CORNERS.itemsize].cpu().numpy().view(QUAD_CORNERS)
+        q = q.reshape(n, self.quad_capacity)
+        return [q[i, : int(st[i]["n_quads"])].copy() for i in range(n)], st
+
+    def release_captures(self):
+        """Frees the frame tables held for captured graphs (after those
+        graphs are destroyed)."""
+        lib.check(self.L.atag_detector_release_captures(self.handle), "atag_detector_release_captures")
 
     def detect(self, frames, formats=None):
         self.enqueue(frames, formats=formats)
@@ -185,6 +203,11 @@ class Detector:
         g = self._dev_bytes
         return {
             "stats": st,
+            "capacities": {"point": int(v.point_capacity), "pair": pc, "cluster": int(v.cluster_capacity),
+                           "cluster_point": int(v.cluster_point_capacity)},
+            "pointers": {n: int(getattr(v, n) or 0) for n, _ in FrameViews._fields_
+                         if n not in ("n_pair_points", "pair_capacity", "point_capacity", "cluster_capacity",
+                                      "cluster_point_capacity", "reserved_")},
             "decimated": g(v.decimated, N).reshape(h, w),
             "thresholded": g(v.thresholded, N).reshape(h, w),
             "labels": g(v.labels, 4 * N).view(np.uint32).reshape(h, w),

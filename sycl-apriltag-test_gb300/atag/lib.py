@@ -7,7 +7,7 @@ import ctypes
 import os
 import re
 
-from .records import ClusterOutputs, ClusterPointC, Config, Frame, FrameViews, LineFitPointC, Tuning
+from .records import ClusterOutputs, ClusterPointC, Config, Frame, FrameViews, LineFitPointC, Limits, Tuning
 
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_ROOT, "lib", "libatag_gb300.so")
@@ -55,6 +55,8 @@ _SIGNATURES = {
     "atag_detect_host": (_ST, [_P, _P, _SZ, _SZ, _P, _SZ, _P, _P]),
     "atag_detector_views": (_ST, [_P, _SZ, ctypes.POINTER(FrameViews)]),
     "atag_detector_keep_intermediates": (_ST, [_P, ctypes.c_int]),
+    "atag_detector_set_limits": (_ST, [_P, ctypes.POINTER(Limits)]),
+    "atag_detector_release_captures": (_ST, [_P]),
     "atag_detector_set_stage_events": (_ST, [_P, ctypes.POINTER(_P), _SZ]),
     "atag_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
     "atag_detector_get_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),

@@ -61,7 +61,16 @@ class FrameViews(ctypes.Structure):
                [(n, ctypes.c_void_p) for n in ("pair_keys", "pair_count", "pair_bbox", "pair_gsum", "pair_pxgx")] + \
                [(n, ctypes.c_void_p) for n in ("cluster_keys", "cluster_bounds", "cluster_extents",
                                                 "cluster_points", "line_fit_points", "peak_count", "peaks",
-                                                "peak_clusters", "peak_extents", "fitted")]
+                                                "peak_clusters", "peak_extents", "fitted")] + \
+               [(n, ctypes.c_uint32) for n in ("point_capacity", "cluster_capacity", "cluster_point_capacity",
+                                                "reserved_")]
+
+
+class Limits(ctypes.Structure):
+    """atag_limits: per-frame capacities and iteration caps (0 = default)."""
+    _fields_ = [(n, ctypes.c_uint32) for n in ("point_capacity", "pair_capacity", "cluster_capacity",
+                                                "cluster_point_capacity", "uf_iteration_cap")] + \
+               [("reserved", ctypes.c_uint32 * 3)]
 
 # device flag bits (atag_frame_stats.status)
 DEVFLAG_POINT_OVERFLOW = 0x1

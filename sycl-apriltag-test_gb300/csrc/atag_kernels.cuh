@@ -67,6 +67,9 @@ struct FrameDesc {
     // DEAD_PAIRS keys (EMPTY = ~0) of pairs whose running point count is
     // already above the cluster size limit; null when not tracked
     unsigned long long* dead_pairs;
+    // iteration cap of the frame-wide union-find loops (0: the bound the
+    // tile count gives, see k_pixels.cu)
+    uint32_t uf_cap;
     // optional (stage entry point): every pair's ClusterBounds and key in
     // key order, up to pair_out_cap entries; null in the fused path
     atag_cluster_bounds* pair_bounds_out;

@@ -199,6 +199,7 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, bool ow
 }
 
 constexpr int RING = 16;
+constexpr int CAPTURE_SLOTS = 16;  // distinct frame tables that captured graphs may hold
 constexpr size_t WORK_LISTS = 5;  // batch-wide work lists of the per-cluster kernels
 constexpr int MAX_LANES = 4;      // sub-batches of one call that run concurrently
 
@@ -270,6 +271,7 @@ struct atag_detector {
     bool owns_ws = false;
     // header carve-out
     FrameDesc* d_tables = nullptr;   // RING x max_frames
+    FrameDesc* d_captured = nullptr; // CAPTURE_SLOTS x max_frames: tables of captured calls
     uint32_t* d_work = nullptr;      // per lane: offsets (WORK_LISTS x (max_frames + 1)) + WORK_LISTS counters
     cudaStream_t lane_stream[MAX_LANES] = {};    // streams of lanes 1.. (lane 0 runs on the caller's)
     cudaStream_t side[MAX_LANES] = {};           // per lane: stream of the large-cluster kernel
@@ -284,6 +286,8 @@ struct atag_detector {
     size_t frames_bytes = 0;
     // host staging for the frame tables
     FrameDesc* h_staging = nullptr;  // pinned, RING x max_frames
+    FrameDesc* h_captured = nullptr; // pinned, CAPTURE_SLOTS x max_frames; never rewritten while in use
+    std::vector<std::vector<FrameDesc>> captured;  // contents of the captured slots in use
     cudaEvent_t ev[RING];
     int ring = 0;
     int last_slot = -1;
@@ -291,6 +295,7 @@ struct atag_detector {
     std::vector<FrameDesc> cur;      // table of the last call
     std::vector<cudaEvent_t> stage_events;
     atag_tuning tuning{16, 16, (int32_t)CF_SMALL_CAP, 8, 2, 8, 2};
+    atag_limits limits{};
     bool keep_intermediates = false;
 };
 
@@ -301,6 +306,7 @@ constexpr size_t HOST_QUAD_CAP = 4096;
 size_t header_bytes(size_t max_frames, size_t input_bytes) {
     size_t b = 0;
     b += al(sizeof(FrameDesc) * RING * max_frames);
+    b += al(sizeof(FrameDesc) * CAPTURE_SLOTS * max_frames);
     b += al(4 * MAX_LANES * (WORK_LISTS * (max_frames + 1) + WORK_LISTS));
     b += al(input_bytes);
     b += al(sizeof(atag_quad_corners) * HOST_QUAD_CAP);
@@ -726,6 +732,7 @@ atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t ma
     }
     char* p = det->ws;
     det->d_tables = (FrameDesc*)p; p += al(sizeof(FrameDesc) * RING * max_frames);
+    det->d_captured = (FrameDesc*)p; p += al(sizeof(FrameDesc) * CAPTURE_SLOTS * max_frames);
     det->d_work = (uint32_t*)p; p += al(4 * MAX_LANES * (WORK_LISTS * (max_frames + 1) + WORK_LISTS));
     det->input_bytes = max_total_pixels * (size_t)c.decimate * (size_t)c.decimate;
     det->d_input = (uint8_t*)p; p += al(det->input_bytes);
@@ -735,7 +742,10 @@ atag_status atag_detector_create(const atag_config* cfg, size_t max_w, size_t ma
     det->frames_base = p;
     det->frames_bytes = det->ws_bytes - (size_t)(p - det->ws);
     cudaError_t e = cudaHostAlloc(&det->h_staging, sizeof(FrameDesc) * RING * max_frames, cudaHostAllocDefault);
+    if (e == cudaSuccess)
+        e = cudaHostAlloc(&det->h_captured, sizeof(FrameDesc) * CAPTURE_SLOTS * max_frames, cudaHostAllocDefault);
     if (e != cudaSuccess) {
+        if (det->h_staging) cudaFreeHost(det->h_staging);
         if (det->owns_ws) cudaFree(det->ws);
         delete det;
         return fail(ATAG_ERR_OUT_OF_MEMORY, "cudaHostAlloc: %s", cudaGetErrorString(e));
@@ -778,13 +788,60 @@ atag_status atag_detector_destroy(atag_detector* det) {
     }
     if (det->lane_fork) cudaEventDestroy(det->lane_fork);
     if (det->h_staging) cudaFreeHost(det->h_staging);
+    if (det->h_captured) cudaFreeHost(det->h_captured);
     if (det->owns_ws) cudaFree(det->ws);
     delete det;
     return ATAG_OK;
 }
 
+// Lowers a frame's capacities to the detector's limits (never raises them:
+// the workspace was laid out for the defaults).
+static void apply_limits(const atag_limits& L, FrameDesc* d) {
+    if (L.point_capacity) d->point_cap = std::min(d->point_cap, L.point_capacity);
+    if (L.pair_capacity) {
+        uint32_t p = 1;
+        while (p * 2 <= std::min(d->pair_cap, L.pair_capacity)) p *= 2;
+        d->pair_cap = p;
+    }
+    if (L.cluster_capacity) d->cluster_cap = std::min(d->cluster_cap, L.cluster_capacity);
+    if (L.cluster_point_capacity) d->cpoint_cap = std::min(d->cpoint_cap, L.cluster_point_capacity);
+    d->uf_cap = L.uf_iteration_cap;
+}
+
+// The device table of frame descriptors a call's kernels read.  Eager calls
+// cycle through a ring of RING slots (a slot is rewritten RING uploads
+// later).  A call being captured into a CUDA graph gets a slot of its own
+// instead, which no later call rewrites: the graph's copy node reloads the
+// same pinned host bytes into it on every replay, so the graph keeps
+// detecting the frames it captured however many eager calls run in between.
+// Captures of identical tables share a slot.
+static atag_status upload_captured(atag_detector* det, const std::vector<FrameDesc>& t, cudaStream_t s,
+                                   const FrameDesc** d_table) {
+    const size_t n = t.size();
+    size_t slot = det->captured.size();
+    for (size_t k = 0; k < det->captured.size(); k++)
+        if (det->captured[k].size() == n && memcmp(det->captured[k].data(), t.data(), n * sizeof(FrameDesc)) == 0)
+            slot = k;
+    if (slot == det->captured.size()) {
+        if (slot == (size_t)CAPTURE_SLOTS)
+            return fail(ATAG_ERR_CAPACITY,
+                        "detect_batch: %d different frame tables are held by captured graphs; destroy those graphs "
+                        "and call atag_detector_release_captures",
+                        CAPTURE_SLOTS);
+        memcpy(det->h_captured + slot * det->max_frames, t.data(), n * sizeof(FrameDesc));
+        det->captured.push_back(t);
+    }
+    FrameDesc* d = det->d_captured + slot * det->max_frames;
+    CK(cudaMemcpyAsync(d, det->h_captured + slot * det->max_frames, n * sizeof(FrameDesc), cudaMemcpyHostToDevice, s));
+    *d_table = d;
+    return ATAG_OK;
+}
+
 static atag_status upload_table(atag_detector* det, const std::vector<FrameDesc>& t, cudaStream_t s,
                                 const FrameDesc** d_table) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return upload_captured(det, t, s, d_table);
     size_t n = t.size();
     if (det->last_slot >= 0 && det->last.size() == n && memcmp(det->last.data(), t.data(), n * sizeof(FrameDesc)) == 0) {
         *d_table = det->d_tables + (size_t)det->last_slot * det->max_frames;
@@ -967,6 +1024,7 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
         d.quad_cap = (uint32_t)quad_cap;
         d.stats = d_stats + i;
         d.stage_outputs = det->keep_intermediates ? 1u : 0u;
+        apply_limits(det->limits, &d);
     }
     const FrameDesc* d_table;
     atag_status st = upload_table(det, t, s, &d_table);
@@ -1061,6 +1119,21 @@ atag_status atag_detector_views(const atag_detector* det, size_t frame, atag_fra
     out->peak_clusters = d.peak_clusters;
     out->peak_extents = d.peak_extents;
     out->fitted = d.fitted;
+    out->point_capacity = d.point_cap;
+    out->cluster_capacity = d.cluster_cap;
+    out->cluster_point_capacity = d.cpoint_cap;
+    return ATAG_OK;
+}
+
+atag_status atag_detector_release_captures(atag_detector* det) {
+    if (!det) return fail(ATAG_ERR_INVALID_ARGUMENT, "release_captures: null detector");
+    det->captured.clear();
+    return ATAG_OK;
+}
+
+atag_status atag_detector_set_limits(atag_detector* det, const atag_limits* limits) {
+    if (!det || !limits) return fail(ATAG_ERR_INVALID_ARGUMENT, "set_limits: null argument");
+    det->limits = *limits;
     return ATAG_OK;
 }
 

@@ -138,8 +138,25 @@ __global__ void __launch_bounds__(256) k_threshold(const __grid_constant__ Frame
 // (3) final labels, and tile counts folded into the component root.
 // ---------------------------------------------------------------------------
 constexpr int CCL_BX = 32;  // blocks per tile row; CCL_BY (8, 16 or 32) rows is a tuning choice
-constexpr uint32_t UF_FIND_CAP = 1u << 23;   // longest parent chain followed
-constexpr uint32_t UF_UNION_CAP = 1u << 12;  // retries of one contended union
+
+// Iteration caps of the union-find loops.  Every union links a root to a
+// smaller slot, so a parent chain strictly decreases and visits each slot at
+// most once.  In a tile's shared-memory forest that bounds a chain by the
+// tile's slots.  In the frame's forest the local pass leaves every slot one
+// step from its tile root, and the border pass only links roots of
+// components that touch a tile edge: at most two (one per colour) per edge
+// block, 2 (2 CCL_BX + 2 rows) edge blocks per tile, largest for 8-row
+// tiles.  So a chain, and the retries of one union (each moves to a
+// strictly smaller root), are bounded by uf_bound(w, h); a loop that gets
+// there flags ATAG_DEVFLAG_UF_ITERATION_CAP instead of spinning.
+// FrameDesc::uf_cap may lower the bound (0 keeps it).
+__device__ __forceinline__ uint32_t uf_bound(uint32_t w, uint32_t h) {
+    const uint32_t tiles = ((w / 2 + CCL_BX - 1) / CCL_BX) * ((h / 2 + 7) / 8);
+    return 2u * (2u * CCL_BX + 2u * 8u) * tiles + 2u;
+}
+__device__ __forceinline__ uint32_t uf_cap_of(const FrameDesc& F) {
+    return F.uf_cap ? F.uf_cap : uf_bound(F.width, F.height);
+}
 
 // Which neighbour blocks (bit 0 P, 1 Q, 2 R, 3 S) a block links to in the
 // 255 forest (wmask) and the 0 forest (bmask); info = pixel colour bits as
@@ -175,26 +192,33 @@ __device__ __forceinline__ BlockLinks block_links(PixelAt px, int x, int y, int 
     return BlockLinks{info, wm, bm};
 }
 
-__device__ __forceinline__ uint32_t find_root_volatile(volatile uint32_t* p, uint32_t n) {
+// Root of n, following at most `cap` parents; *capped is set when the cap
+// ends the walk before a root.
+__device__ __forceinline__ uint32_t find_root_volatile(volatile uint32_t* p, uint32_t n, uint32_t cap, bool* capped) {
     // path halving: every write replaces a parent by one of its ancestors,
     // which stays valid under concurrent unions (only roots are re-linked)
-    for (uint32_t it = 0; it < UF_FIND_CAP; it++) {
+    for (uint32_t it = 0; it < cap; it++) {
         uint32_t q = p[n];
         if (q == n) return n;
         uint32_t g = p[q];
         if (g != q) p[n] = g;
         n = g;
     }
+    *capped = true;
     return n;
 }
 
-// Lock-free union toward the smaller root (union_find.h:50-77) with an
-// iteration cap; returns false if the cap was hit.
+// Lock-free union toward the smaller root (union_find.h:50-77) with
+// iteration caps; returns false if a cap was hit.  With a non-root in hand
+// the union still only lowers parents (atomicMin), so the forest stays
+// acyclic and every later walk ends.
 template <typename Ptr>
-__device__ __forceinline__ bool uf_union(Ptr par, uint32_t a, uint32_t b) {
-    for (uint32_t it = 0; it < UF_UNION_CAP; it++) {
-        a = find_root_volatile(par, a);
-        b = find_root_volatile(par, b);
+__device__ __forceinline__ bool uf_union(Ptr par, uint32_t a, uint32_t b, uint32_t cap) {
+    bool capped = false;
+    for (uint32_t it = 0; it < cap; it++) {
+        a = find_root_volatile(par, a, cap, &capped);
+        b = find_root_volatile(par, b, cap, &capped);
+        if (capped) return false;
         if (a == b) return true;
         if (a < b) {
             uint32_t old = atomicMin((uint32_t*)&par[b], a);
@@ -330,12 +354,13 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
         for (uint32_t k = lane; k < total; k += 32) {
             const uint32_t e = ulist[ty][k];
-            uf_union((volatile uint32_t*)par, e >> 16, e & 0xFFFFu);
+            uf_union((volatile uint32_t*)par, e >> 16, e & 0xFFFFu, 2u * CCL_THREADS);
         }
     }
     __syncthreads();
-    uint32_t rw = find_root_volatile((volatile uint32_t*)par, 2 * l);
-    uint32_t rb = find_root_volatile((volatile uint32_t*)par, 2 * l + 1);
+    bool local_capped = false;  // cannot happen: a tile chain visits at most its 2 CCL_THREADS slots
+    uint32_t rw = find_root_volatile((volatile uint32_t*)par, 2 * l, 2u * CCL_THREADS, &local_capped);
+    uint32_t rb = find_root_volatile((volatile uint32_t*)par, 2 * l + 1, 2u * CCL_THREADS, &local_capped);
     // pixel counts per root: the blocks of a run share its root, so the
     // run's last lane adds the run's count (segmented warp sum)
     {
@@ -385,6 +410,7 @@ __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
     volatile uint32_t* par = F.scratch;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ uint2 blist[8][8 * 32];  // per warp: the unions of one pass (8 per lane at most)
+    const uint32_t cap = uf_cap_of(F);
     bool ok = true;
     // warp-uniform trip count: lanes past the end take part in the votes
     for (int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < total; i0 += gridDim.x * blockDim.x) {
@@ -444,7 +470,7 @@ __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
         const uint32_t nlist = __shfl_sync(0xFFFFFFFFu, incl, 31);
         for (uint32_t k = (uint32_t)lane; k < nlist; k += 32) {
             const uint2 e = blist[warp][k];
-            ok &= uf_union(par, e.x, e.y);
+            ok &= uf_union(par, e.x, e.y, cap);
         }
         __syncwarp();
     }
@@ -463,6 +489,7 @@ __global__ void __launch_bounds__(256, 8) k_ccl_final(const __grid_constant__ Fr
     const int w = F.width, h = F.height;
     const int npx = w / 4, np = npx * (h / 2);  // block pairs (w % 4 == 0)
     const uint32_t* par = F.scratch;
+    const uint32_t cap = uf_cap_of(F);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
         const int px = i % npx, by = i / npx;
         const size_t id = (size_t)(by * 2) * w + (size_t)px * 4;
@@ -472,7 +499,7 @@ __global__ void __launch_bounds__(256, 8) k_ccl_final(const __grid_constant__ Fr
         const uint32_t bot = *reinterpret_cast<const uint32_t*>(F.thr + id + w);
         uint32_t r[4] = {p4.x, p4.y, p4.z, p4.w};
         bool capped = true;
-        for (uint32_t it = 0; it < UF_FIND_CAP; it++) {
+        for (uint32_t it = 0; it < cap; it++) {
             uint32_t q[4];
 #pragma unroll
             for (int k = 0; k < 4; k++) q[k] = par[r[k]];
