@@ -16,7 +16,8 @@ interface (`launch`, `done`, `results`), so its logic is tested on the CPU
 with a fake executor and run on the GPU with DetectorExecutor.
 """
 import collections
-import heapq
+import contextlib
+import gc
 import time
 from dataclasses import dataclass, field
 
@@ -216,6 +217,29 @@ def poisson_arrivals(rates_hz, duration_s, seed):
     return heap
 
 
+@contextlib.contextmanager
+def latency_critical():
+    """For the length of a serving run: one full garbage collection up front,
+    then the objects that exist are frozen out of the collector's reach, so
+    the collections that run during the loop only scan what the loop itself
+    allocates (a full collection over a large process can stall the loop
+    for milliseconds)."""
+    gc.collect()
+    gc.freeze()
+    try:
+        yield
+    finally:
+        gc.unfreeze()
+
+
+def warm(server: Server, frame):
+    """Runs one frame through every slot before the clock starts (the first
+    launch on a slot pays for lazy kernel loading and first-touch costs)."""
+    for ex in server.slots:
+        ex.launch([frame])
+        ex.results()
+
+
 def run_cameras(server: Server, camera_frames, rates_hz, duration_s, seed=0, on_result=None):
     """Replays Poisson arrivals in real time: camera c submits
     camera_frames[c][k % len] at each of its arrival times.  Returns the
@@ -223,16 +247,41 @@ def run_cameras(server: Server, camera_frames, rates_hz, duration_s, seed=0, on_
     arrivals = poisson_arrivals(rates_hz, duration_s, seed)
     counters = collections.Counter()
     seq = 0
-    server.t0 = server.clock()
-    for t, cam in arrivals:
-        while server.now() < t:
+    with latency_critical():
+        server.t0 = server.clock()
+        for t, cam in arrivals:
+            while server.now() < t:
+                server.poll()
+            frames = camera_frames[cam]
+            server.submit(Request(seq, cam, frames[counters[cam] % len(frames)], server.now()))
+            counters[cam] += 1
+            seq += 1
             server.poll()
-        frames = camera_frames[cam]
-        server.submit(Request(seq, cam, frames[counters[cam] % len(frames)], server.now()))
-        counters[cam] += 1
-        seq += 1
-        server.poll()
-    server.drain()
+        server.drain()
+    return sorted(server.completed, key=lambda r: r.seq)
+
+
+def run_bursts(server: Server, camera_frames, n_bursts, burst_size, period_s, on_result=None):
+    """Bursts of burst_size simultaneous requests (cameras taken in turn)
+    every period_s seconds, e.g. a rig of cameras triggered together.
+    Returns the completed results sorted by sequence number."""
+    counters = collections.Counter()
+    seq = 0
+    with latency_critical():
+        server.t0 = server.clock()
+        for b in range(n_bursts):
+            t = b * period_s
+            while server.now() < t:
+                server.poll()
+            now = server.now()
+            for k in range(burst_size):
+                cam = seq % len(camera_frames)
+                frames = camera_frames[cam]
+                server.submit(Request(seq, cam, frames[counters[cam] % len(frames)], now))
+                counters[cam] += 1
+                seq += 1
+            server.poll()
+        server.drain()
     return sorted(server.completed, key=lambda r: r.seq)
 
 
@@ -240,4 +289,5 @@ def latency_summary(results, duration_s):
     lat = np.array([r.latency_ms for r in results]) if results else np.zeros(1)
     return {"requests": len(results), "frames_per_s": len(results) / duration_s,
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "max_ms": float(lat.max()), "mean_batch": float(np.mean([r.batch_size for r in results]) if results else 0)}
+            "max_ms": float(lat.max()), "mean_batch": float(np.mean([r.batch_size for r in results]) if results else 0),
+            "max_batch": int(max((r.batch_size for r in results), default=0))}
