@@ -465,6 +465,15 @@ typedef struct atag_limits {
 } atag_limits;
 atag_status atag_detector_set_limits(atag_detector *det, const atag_limits *limits);
 
+/* Subpixel refinement of the detected corners (no counterpart in the
+ * reference, whose corners are the FP64 intersections of its line fits,
+ * src/main.cpp:1059-1099).  When enabled, later detect calls end with one
+ * more stage that replaces each quad's corners, in place, by
+ * atag_refine_forward's refined corners computed on the frame's grey image
+ * (as value / 255); a corner whose adjacent edge lines are nearly parallel
+ * keeps its position.  Off by default: the quads are then the reference's. */
+atag_status atag_detector_set_refinement(atag_detector *det, int enable);
+
 /* Frees the frame-table copies held for captured calls; call it once every
  * graph captured from this detector has been destroyed. */
 atag_status atag_detector_release_captures(atag_detector *det);
@@ -609,7 +618,7 @@ atag_status atag_detector_set_tuning(atag_detector *det, const atag_tuning *tuni
  * after the last, so cudaEventElapsedTime(events[i], events[i+1]) is stage
  * i's device time.  Pass NULL / 0 to stop.  The reference prints cumulative
  * per-stage wall times instead (src/main.cpp:330-977). */
-#define ATAG_STAGE_COUNT 15
+#define ATAG_STAGE_COUNT 16
 atag_status atag_detector_set_stage_events(atag_detector *det, void *const *events, size_t n_events);
 /* Name of stage i (e.g. "ccl_local"), or NULL past the last. */
 const char *atag_stage_name(int stage);

@@ -115,6 +115,11 @@ class Detector:
         q = q.reshape(n, self.quad_capacity)
         return [q[i, : int(st[i]["n_quads"])].copy() for i in range(n)], st
 
+    def set_refinement(self, enable: bool = True):
+        """Later calls replace each quad's corners by their subpixel
+        refinement on the frame's grey image (atag_detector_set_refinement)."""
+        lib.check(self.L.atag_detector_set_refinement(self.handle, 1 if enable else 0), "atag_detector_set_refinement")
+
     def release_captures(self):
         """Frees the frame tables held for captured graphs (after those
         graphs are destroyed)."""

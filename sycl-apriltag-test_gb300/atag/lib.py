@@ -57,6 +57,7 @@ _SIGNATURES = {
     "atag_detector_keep_intermediates": (_ST, [_P, ctypes.c_int]),
     "atag_detector_set_limits": (_ST, [_P, ctypes.POINTER(Limits)]),
     "atag_detector_release_captures": (_ST, [_P]),
+    "atag_detector_set_refinement": (_ST, [_P, ctypes.c_int]),
     "atag_detector_set_stage_events": (_ST, [_P, ctypes.POINTER(_P), _SZ]),
     "atag_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
     "atag_detector_get_tuning": (_ST, [_P, ctypes.POINTER(Tuning)]),
@@ -66,7 +67,7 @@ _SIGNATURES = {
     "atag_estimate_pose": (_ST, [_P, _SZ, _SZ, _D, _D, _D, _D, _D, _U32, _P, _P]),
     "atag_decode_quads": (_ST, [_P, _SZ, _SZ, _SZ, _P, _SZ, _SZ, _P, _SZ, _U32, _U32, _D, _P, _P]),
 }
-STAGE_COUNT = 15
+STAGE_COUNT = 16
 
 _lib = None
 

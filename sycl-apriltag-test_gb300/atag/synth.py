@@ -148,8 +148,21 @@ def _blur(img, sigma):
     return out2
 
 
-def render(spec: FrameSpec, seed: int) -> np.ndarray:
-    """Renders one uint8 frame of spec.height x spec.width from `seed`."""
+def border_corners(quad):
+    """The outer corners of a rendered tag's black border (cells 1 and 9 of
+    its 10-cell square), with pixel centres at integer coordinates: where
+    the detector's quad corners should lie."""
+    H = _homography(np.array([[0, 0], [10, 0], [10, 10], [0, 10]], np.float64), quad)
+    inner = np.array([[1, 1, 1], [9, 1, 1], [9, 9, 1], [1, 9, 1]], np.float64)
+    p = inner @ H.T
+    return p[:, :2] / p[:, 2:] - 0.5
+
+
+def render(spec: FrameSpec, seed: int, truth: list = None) -> np.ndarray:
+    """Renders one uint8 frame of spec.height x spec.width from `seed`.
+    If `truth` is a list, the border corners (border_corners) of every tag
+    are appended to it in drawing order (later tags may cover earlier
+    ones); the pixels do not depend on it."""
     rng = np.random.default_rng(seed)
     h, w = spec.height, spec.width
     img = rng.uniform(90, 170, size=(h, w)).astype(np.float32)
@@ -166,6 +179,8 @@ def render(spec: FrameSpec, seed: int) -> np.ndarray:
         quad = _tag_quad(rng, cx, cy, side, spec.max_tilt_deg)
         bits = rng.random((6, 6)) < 0.5
         _render_tag(img, rng, quad, bits)
+        if truth is not None:
+            truth.append(border_corners(quad))
     img = _blur(img, rng.uniform(*spec.blur_sigma))
     img += rng.normal(0, rng.uniform(*spec.noise_sigma), size=img.shape).astype(np.float32)
     if spec.salt_pepper > 0:

@@ -192,6 +192,9 @@ __global__ void k_index_quads(const __grid_constant__ FrameSet fs, const uint32_
                               PipelineParams p);
 __global__ void k_compact_quads(const __grid_constant__ FrameSet fs);
 
+// k_refine.cu: refinement of the detector's quads in place (optional stage)
+__global__ void k_refine_detected(const __grid_constant__ FrameSet fs);
+
 // k_stage_cluster.cu (stage entry points over the dense boundary planes)
 __global__ void k_planes_pairs(const __grid_constant__ FrameSet fs, const uint32_t* __restrict__ points,
                                const unsigned long long* __restrict__ keys, uint32_t n);

@@ -297,6 +297,7 @@ struct atag_detector {
     atag_tuning tuning{16, 16, (int32_t)CF_SMALL_CAP, 8, 2, 8, 2};
     atag_limits limits{};
     bool keep_intermediates = false;
+    bool refine = false;
 };
 
 namespace {
@@ -985,6 +986,11 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
     k_compact_quads<<<(unsigned)n, 1024, 0, s>>>(fs);
     LAUNCHED();
     STAGE(15);
+    if (det->refine) {
+        k_refine_detected<<<dim3((unsigned)n, 64), 128, 0, s>>>(fs);
+        LAUNCHED();
+    }
+    STAGE(16);
 #undef STAGE
     return ATAG_OK;
 }
@@ -1125,6 +1131,12 @@ atag_status atag_detector_views(const atag_detector* det, size_t frame, atag_fra
     return ATAG_OK;
 }
 
+atag_status atag_detector_set_refinement(atag_detector* det, int enable) {
+    if (!det) return fail(ATAG_ERR_INVALID_ARGUMENT, "set_refinement: null detector");
+    det->refine = enable != 0;
+    return ATAG_OK;
+}
+
 atag_status atag_detector_release_captures(atag_detector* det) {
     if (!det) return fail(ATAG_ERR_INVALID_ARGUMENT, "release_captures: null detector");
     det->captured.clear();
@@ -1179,7 +1191,7 @@ const char* atag_stage_name(int i) {
     static const char* names[ATAG_STAGE_COUNT] = {
         "reset", "decimate", "threshold", "ccl_local", "ccl_border", "ccl_final", "boundaries_pairs",
         "pairs_finalize", "scatter_points", "cluster_sort", "cluster_errors", "cluster_peaks", "peaks_scan",
-        "index_quads", "compact_quads"};
+        "index_quads", "compact_quads", "refine"};
     return (i >= 0 && i < ATAG_STAGE_COUNT) ? names[i] : nullptr;
 }
 

@@ -37,15 +37,27 @@ struct Bilinear {
     float v, gx, gy;  // value and its spatial gradient
 };
 
-__device__ __forceinline__ Bilinear bilinear(const float* __restrict__ img, int w, int h, float x, float y) {
+// Pixel sources: an FP32 image, or the detector's u8 grey frame read as
+// value / 255 (the same numbers as the FP32-normalised image).
+struct F32Image {
+    const float* __restrict__ p;
+    __device__ __forceinline__ float operator[](size_t i) const { return __ldg(p + i); }
+};
+struct U8Image {
+    const uint8_t* __restrict__ p;
+    __device__ __forceinline__ float operator[](size_t i) const { return __fdiv_rn((float)__ldg(p + i), 255.0f); }
+};
+
+template <class Img>
+__device__ __forceinline__ Bilinear bilinear(const Img& img, int w, int h, float x, float y) {
     const float xc = fminf(fmaxf(x, 0.0f), (float)(w - 1)), yc = fminf(fmaxf(y, 0.0f), (float)(h - 1));
     const bool inx = x > 0.0f && x < (float)(w - 1), iny = y > 0.0f && y < (float)(h - 1);
     int x0 = (int)floorf(xc), y0 = (int)floorf(yc);
     x0 = min(x0, w - 2);
     y0 = min(y0, h - 2);
     const float fx = xc - (float)x0, fy = yc - (float)y0;
-    const float i00 = __ldg(img + (size_t)y0 * w + x0), i01 = __ldg(img + (size_t)y0 * w + x0 + 1);
-    const float i10 = __ldg(img + (size_t)(y0 + 1) * w + x0), i11 = __ldg(img + (size_t)(y0 + 1) * w + x0 + 1);
+    const float i00 = img[(size_t)y0 * w + x0], i01 = img[(size_t)y0 * w + x0 + 1];
+    const float i10 = img[(size_t)(y0 + 1) * w + x0], i11 = img[(size_t)(y0 + 1) * w + x0 + 1];
     Bilinear b;
     b.v = (1.0f - fy) * ((1.0f - fx) * i00 + fx * i01) + fy * ((1.0f - fx) * i10 + fx * i11);
     b.gx = inx ? (1.0f - fy) * (i01 - i00) + fy * (i11 - i10) : 0.0f;
@@ -82,7 +94,8 @@ struct LaneState {
     float nux, nuy, dist;  // normal of the fitted line, distance of q_j to it
 };
 
-__device__ __forceinline__ void edge_forward(const float* __restrict__ img, int iw, int ih, float ax, float ay, float bx,
+template <class Img>
+__device__ __forceinline__ void edge_forward(const Img& img, int iw, int ih, float ax, float ay, float bx,
                                              float by, LaneState& L, EdgeLine& E) {
     const int lane = threadIdx.x & 31, j = lane >> 1, half = lane & 1;
     L.ax = ax; L.ay = ay; L.bx = bx; L.by = by;
@@ -187,7 +200,7 @@ __global__ void __launch_bounds__(128) k_refine_forward(const float* __restrict_
     const int e1 = (e + 1) & 3;
     LaneState L;
     EdgeLine E;
-    edge_forward(img, iw, ih, c[2 * e], c[2 * e + 1], c[2 * e1], c[2 * e1 + 1], L, E);
+    edge_forward(F32Image{img}, iw, ih, c[2 * e], c[2 * e + 1], c[2 * e1], c[2 * e1 + 1], L, E);
     if (samples) {
         const int j = lane >> 1, half = lane & 1;
         float* s = samples + ((size_t)q * 4 + e) * (RF_POS * RF_TAPS) + j * RF_TAPS + 2 * half;
@@ -208,6 +221,41 @@ __global__ void __launch_bounds__(128) k_refine_forward(const float* __restrict_
     }
 }
 
+// Refinement of the detector's own quads, in place, as the last stage of a
+// detect call: the frame's u8 grey image, read as value / 255, gives the
+// same refined corners as atag_refine_forward on the FP32-normalised image.
+// A corner whose two edge lines are nearly parallel (|sin| of their angle
+// at most 1e-3) keeps its unrefined position.  Frame blockIdx.x; its quads
+// blockIdx.y, blockIdx.y + gridDim.y, ...
+__global__ void __launch_bounds__(128) k_refine_detected(const __grid_constant__ FrameSet fs) {
+    __shared__ EdgeLine lines[4];
+    __shared__ float s_c[8];
+    const FrameDesc& F = fs.get(blockIdx.x);
+    const uint32_t nq = min(F.stats->n_quads, F.quad_cap);
+    const U8Image img{F.grey};
+    const int e = threadIdx.x >> 5, lane = threadIdx.x & 31, e1 = (e + 1) & 3;
+    for (uint32_t q = blockIdx.y; q < nq; q += gridDim.y) {
+        atag_quad_corners* qc = F.quads + q;
+        if (threadIdx.x < 8) s_c[threadIdx.x] = qc->corners[threadIdx.x >> 1][threadIdx.x & 1];
+        __syncthreads();
+        LaneState L;
+        EdgeLine E;
+        edge_forward(img, (int)F.width, (int)F.height, s_c[2 * e], s_c[2 * e + 1], s_c[2 * e1], s_c[2 * e1 + 1], L, E);
+        if (lane == 0) lines[e] = E;
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            const int i = threadIdx.x;
+            double cx, cy, alpha, P, Q;
+            intersect(lines[(i + 3) & 3], lines[i], cx, cy, alpha, P, Q);
+            if (fabs(Q) > 1e-3 && isfinite(cx) && isfinite(cy)) {
+                qc->corners[i][0] = (float)cx;
+                qc->corners[i][1] = (float)cy;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(128) k_refine_backward(const float* __restrict__ img, int iw, int ih,
                                                          const float* __restrict__ corners, int nq,
                                                          const float* __restrict__ g_refined,
@@ -224,7 +272,7 @@ __global__ void __launch_bounds__(128) k_refine_backward(const float* __restrict
     const int e1 = (e + 1) & 3;
     LaneState L;
     EdgeLine E;
-    edge_forward(img, iw, ih, c[2 * e], c[2 * e + 1], c[2 * e1], c[2 * e1 + 1], L, E);
+    edge_forward(F32Image{img}, iw, ih, c[2 * e], c[2 * e + 1], c[2 * e1], c[2 * e1 + 1], L, E);
     if (lane == 0) lines[e] = E;
     if (threadIdx.x < 8) {
         (&gm[0][0])[threadIdx.x] = 0.0;
