@@ -71,7 +71,8 @@ def camera_specs():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+    """nvidia-smi clocks/throttle sampling (every 50 ms) during the timed
+    region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -86,7 +87,7 @@ class ClockSampler:
         os.close(fd)
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", str(self.dev)], stdout=open(self.path, "w"),
+                                          "-lms", "50", "-i", str(self.dev)], stdout=open(self.path, "w"),
                                          stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
@@ -148,6 +149,34 @@ def stage_bytes(stats, n_src_px):
     }
 
 
+def survey_bytes(stats):
+    """Algorithmic bytes per stage from the survey's per-unit figures (its
+    measurement table), for the whole batch: N pixels, P boundary points,
+    C pairs, P_f points of surviving clusters, K corner peaks, C_p clusters
+    with peaks.  A fused kernel is charged the rows of the reference stages
+    it replaces that read or write HBM in the reference; for
+    boundaries_pairs that is the find_boundaries row, 4N + 4N + 12P (labels,
+    size gathers bounded by N words, the points and keys), leaving out the
+    pair sort and bounds reduction rows it also replaces."""
+    N = sum(int(s["width"]) * int(s["height"]) for s in stats)
+    P = sum(int(s["n_points"]) for s in stats)
+    C = sum(int(s["n_pairs"]) for s in stats)
+    Pf = sum(int(s["n_cluster_points"]) for s in stats)
+    K = sum(int(s["n_corners"]) for s in stats)
+    Cp = sum(int(s["n_peak_clusters"]) for s in stats)
+    return {
+        "threshold": 2 * N,
+        "ccl_local": N + 4 * N,
+        "boundaries_pairs": 4 * N + 4 * N + 12 * P,
+        "pairs_finalize": 32 * C,
+        "scatter_points": 12 * P + 32 * C + 10 * Pf,
+        "cluster_sort": 2 * 10 * Pf + (8 + 4 + 48) * Pf + 2 * 48 * Pf,
+        "cluster_errors": 48 * Pf * 2 + 2 * Pf + 12 * K,
+        "cluster_peaks": 2 * 12 * K,
+        "index_quads": Cp * (8 + 120 + 4 * 2 * 48) + 272 * Cp,
+    }
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -170,7 +199,7 @@ def plain_path(args, det1, frames, stream):
     """Single-frame latency: one graph replay per frame, the L2 flushed by a
     256 MB write before each frame."""
     import torch
-    inp = torch.empty((H, W), dtype=torch.uint8, device="cuda")
+    inp = torch.empty(tuple(frames[0].shape), dtype=torch.uint8, device="cuda")
     inp.copy_(frames[0])
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -199,6 +228,35 @@ def plain_path(args, det1, frames, stream):
             "mean_ms": statistics.mean(lat), "frames": len(lat), "l2": "flushed (256 MB write) before each frame"}
 
 
+def graph_ms(args, det, frames, stream, steps):
+    """Device time per replay of one captured detect call over `frames`."""
+    import torch
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            det.enqueue(frames, stream=stream)
+    stream.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        det.enqueue(frames, stream=stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            g.replay()
+        a.record(stream)
+        for _ in range(steps):
+            g.replay()
+        b.record(stream)
+    b.synchronize()
+    del g
+    return a.elapsed_time(b) / steps
+
+
+def per_frame_counts(stats):
+    return {k: statistics.mean(int(s[f]) for s in stats) for k, f in
+            (("points", "n_points"), ("pairs", "n_pairs"), ("clusters", "n_clusters"),
+             ("cluster_points", "n_cluster_points"), ("quads", "n_quads"))}
+
+
 def run_reference(args, rank):
     """The reference arm: the CPU restatement of the reference path on all
     host threads, each step a bounded sample of the same workload."""
@@ -212,6 +270,13 @@ def run_reference(args, rank):
     cfg = oracle.default_config(decimate=args.decimate)
     for _ in range(args.warmup):
         oracle.detect_many(frames[:2], cfg)
+    # the GPU arm's 64 frames per step, unless that would take the K timed
+    # steps past the time budget: then the sample shrinks (and says so)
+    t0 = time.perf_counter()
+    oracle.detect_many(frames[:16], cfg, threads=0)
+    rate = 16 / (time.perf_counter() - t0)
+    if args.steps * len(frames) / rate > args.ref_budget_s:
+        frames = frames[: max(8, int(args.ref_budget_s * rate / args.steps))]
     t0 = time.perf_counter()
     used = 0
     for _ in range(args.steps):
@@ -242,11 +307,20 @@ def main():
     ap.add_argument("--plain-frames", type=int, default=64)
     ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="minimum CPU-baseline timing")
-    ap.add_argument("--ref-sample", type=int, default=16)
+    ap.add_argument("--ref-sample", type=int, default=64, help="frames per step of the reference arm (the GPU "
+                    "arm's batch)")
+    ap.add_argument("--ref-budget-s", type=float, default=150.0, help="time budget of the reference arm's timed "
+                    "steps; a smaller per-step sample is used past it")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--mixed", type=int, default=64, help="frames of the mixed-resolution batch (0 = skip)")
     ap.add_argument("--refine-quads", type=int, default=4096, help="quads of the refinement, pose and tag-reading steps (0 = skip)")
-    ap.add_argument("--serving-seconds", type=float, default=5.0, help="length of the serving run (0 = skip)")
+    ap.add_argument("--serving-seconds", type=float, default=60.0, help="length of the serving run at the "
+                    "cameras' rates (0 = skip)")
+    ap.add_argument("--overload-seconds", type=float, default=2.0, help="length of the serving run at 16x the "
+                    "cameras' rates (0 = skip)")
+    ap.add_argument("--stress-frames", type=int, default=8, help="3840x2160 stress frames per step (0 = skip)")
+    ap.add_argument("--vga-frames", type=int, default=32, help="640x480 frames of the CPU-path configuration "
+                    "(0 = skip)")
     ap.add_argument("--no-tune", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -266,6 +340,11 @@ def main():
         host_frames = list(pool.map(_render, [1000 + k for k in replicas.job_frames(n_render, world, rank)]))
         specs = mixed_specs(extra_n, 77) if extra_n else []
         mixed_frames = list(pool.map(_render_spec, [(sp, 5000 + i) for i, sp in enumerate(specs)]))
+        from atag import synth
+        n4k = args.stress_frames if world == 1 else 0
+        stress_frames = list(pool.map(_render_spec, [(synth.CONFIGS["4k"], 7000 + i) for i in range(n4k)]))
+        nvga = args.vga_frames if world == 1 else 0
+        vga_frames = list(pool.map(_render_spec, [(synth.CONFIGS["vga"], 8000 + i) for i in range(nvga)]))
         cam_frames = []
         if args.serving_seconds > 0 and world == 1:
             cs = camera_specs()
@@ -347,14 +426,22 @@ def main():
         det.set_stage_events(None)
     stage_ms = {k: v / args.steps for k, v in acc.items()}
     sbytes = stage_bytes(stats, B * W * H)
-    dom = max((k for k in stage_ms if k in sbytes and sbytes[k] > 0), key=lambda k: stage_ms[k])
+    vbytes = survey_bytes(stats)
+    dom = max((k for k in stage_ms if k in vbytes and vbytes[k] > 0), key=lambda k: stage_ms[k])
     peak, peak_kind = peaks()
-    achieved = sbytes[dom] / (stage_ms[dom] / 1000.0) / 1e9
+    achieved = vbytes[dom] / (stage_ms[dom] / 1000.0) / 1e9
+    own = sbytes.get(dom, 0) / (stage_ms[dom] / 1000.0) / 1e9
     traffic = ncu_traffic(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": sbytes[dom],
-                "traffic": (traffic * B if traffic is not None else None)}
+                "algorithmic_bytes_per_launch": vbytes[dom],
+                "bytes_formula": "survey per-unit figures (boundaries_pairs: 4N + 4N + 12P)",
+                "kernel_own": {"bytes_per_launch": sbytes.get(dom), "achieved": own, "frac": own / peak,
+                               "formula": "the kernel's own contract (boundaries_pairs: 4N + 8P_f)"},
+                "traffic": (traffic * B if traffic is not None else None),
+                "stages": {k: {"ms": stage_ms[k], "survey_gbs": vbytes[k] / (stage_ms[k] / 1000.0) / 1e9,
+                               "own_gbs": sbytes.get(k, 0) / (stage_ms[k] / 1000.0) / 1e9}
+                           for k in vbytes if stage_ms.get(k, 0) > 0}}
 
     # --- plain single-frame path: latency per frame, L2 flushed in between
     plain = plain_path(args, Detector(w, h, config=cfg), frames, stream) if args.plain_frames > 0 else None
@@ -467,16 +554,67 @@ def main():
                  "tuning": mtune["tuning"] if mtune else None}
         del detm, gm
 
-    # --- corner refinement: forward + hand-written adjoint on 4096 quads
+    # --- the other configurations: 1080p at decimate 2 (the same frames,
+    # decimated in the graph), the 3840x2160 stress frames at decimate 1,
+    # and 640x480 at decimate 2 (the reference's CPU-path configuration)
+    configs = {}
+    cfg2 = lib.default_config(decimate=2)
+    det_d2 = Detector(W // 2, H // 2, max_frames=B, max_total_pixels=B * (W // 2) * (H // 2), config=cfg2)
+    if not args.no_tune:
+        from atag import autotune
+        autotune.autotune(det_d2, frames, reps=2, passes=1)
+    ms_d2 = graph_ms(args, det_d2, frames, stream, args.steps)
+    plain_d2 = plain_path(args, Detector(W // 2, H // 2, config=cfg2), frames, stream) if args.plain_frames else None
+    configs["1080p_d2"] = {"frames_per_step": B, "ms_per_step": ms_d2, "frames_per_s": 1000.0 * B / ms_d2,
+                           "plain": plain_d2, "per_frame": per_frame_counts(det_d2.stats()),
+                           "status_ok": all(int(x["status"]) == 0 for x in det_d2.stats())}
+    del det_d2
+    if stress_frames:
+        sf = [torch.from_numpy(f).cuda() for f in stress_frames]
+        det4 = Detector(3840, 2160, max_frames=len(sf), max_total_pixels=len(sf) * 3840 * 2160, config=cfg)
+        ms4 = graph_ms(args, det4, sf, stream, max(3, args.steps // 8))
+        st4 = det4.stats()
+        configs["4k_stress_d1"] = {"frames_per_step": len(sf), "ms_per_step": ms4,
+                                   "frames_per_s": 1000.0 * len(sf) / ms4,
+                                   "plain": plain_path(args, Detector(3840, 2160, config=cfg), sf, stream)
+                                   if args.plain_frames else None,
+                                   "per_frame": per_frame_counts(st4),
+                                   "status_ok": all(int(x["status"]) == 0 for x in st4)}
+        del det4, sf
+    if vga_frames:
+        vf = [torch.from_numpy(f).cuda() for f in vga_frames]
+        detv = Detector(320, 240, max_frames=len(vf), max_total_pixels=len(vf) * 320 * 240, config=cfg2)
+        msv = graph_ms(args, detv, vf, stream, args.steps)
+        configs["vga_d2"] = {"frames_per_step": len(vf), "ms_per_step": msv, "frames_per_s": 1000.0 * len(vf) / msv,
+                             "plain": plain_path(args, Detector(320, 240, config=cfg2), vf, stream)
+                             if args.plain_frames else None,
+                             "per_frame": per_frame_counts(detv.stats())}
+        del detv, vf
+
+    # --- detection with the corner refinement stage (the same 64-frame step)
+    det_r = Detector(w, h, max_frames=B, max_total_pixels=B * w * h, config=cfg)
+    det_r.set_tuning(**det.get_tuning())
+    det_r.set_refinement(True)
+    ms_r = graph_ms(args, det_r, frames, stream, args.steps)
+    configs["1080p_d1_refined"] = {"frames_per_step": B, "ms_per_step": ms_r, "frames_per_s": 1000.0 * B / ms_r}
+    del det_r
+
+    # --- corner refinement: forward + hand-written adjoint on 4096 detected
+    # quads (the batch's quads, repeated up to 4096, on the batch's frames
+    # stacked into one tall FP32 image)
     refine_line = pose_line = decode_line = None
     if args.refine_quads > 0:
         from atag import refine
         g = torch.Generator(device="cpu").manual_seed(3)
-        img = torch.from_numpy(host_frames[0]).float().div(255.0).cuda()
+        fq, _ = det.results()
+        img = torch.cat(frames, 0).float().div(255.0)
+        rows = [q["corners"] + np.array([0.0, H * f], np.float32) for f, q in enumerate(fq)]
+        found = np.concatenate(rows, 0)
         nq = args.refine_quads
-        ctr = torch.rand((nq, 1, 2), generator=g) * torch.tensor([W - 200.0, H - 200.0]) + 100.0
-        sq = torch.tensor([[-1.0, -1.0], [1.0, -1.0], [1.0, 1.0], [-1.0, 1.0]])
-        quads_c = (ctr + sq[None] * (torch.rand((nq, 1, 1), generator=g) * 40 + 10)).cuda()
+        quads_c = torch.from_numpy(np.resize(found, (nq, 4, 2)).astype(np.float32)).cuda()
+        # the same quads in their own frame's coordinates (pose)
+        quads_local = torch.from_numpy(np.resize(np.concatenate([q["corners"] for q in fq], 0),
+                                                 (nq, 4, 2)).astype(np.float32)).cuda()
         gref = torch.randn((nq, 4, 2), generator=g).cuda()
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):
@@ -490,18 +628,18 @@ def main():
             b.record(stream)
         b.synchronize()
         rms = a.elapsed_time(b) / args.steps
-        refine_line = {"quads": nq, "samples_per_quad": 256, "ms_fwd_bwd": rms,
-                       "quads_per_s": nq / (rms / 1000.0)}
+        refine_line = {"quads": nq, "distinct_detected_quads": int(len(found)), "samples_per_quad": 256,
+                       "ms_fwd_bwd": rms, "quads_per_s": nq / (rms / 1000.0)}
 
         # --- tag pose of the same quads (FP64 homography + Levenberg-Marquardt)
         from atag import pose
         cam = (1000.0, 1000.0, W / 2.0, H / 2.0)
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):
-                poses = pose.estimate_pose(quads_c, *cam, 0.16, stream=stream)
+                poses = pose.estimate_pose(quads_local, *cam, 0.16, stream=stream)
             a.record(stream)
             for _ in range(args.steps):
-                poses = pose.estimate_pose(quads_c, *cam, 0.16, stream=stream)
+                poses = pose.estimate_pose(quads_local, *cam, 0.16, stream=stream)
             b.record(stream)
         b.synchronize()
         pms = a.elapsed_time(b) / args.steps
@@ -515,12 +653,13 @@ def main():
         from atag import decode
         fam = torch.randint(0, 1 << 36, (587,), generator=g, dtype=torch.int64).cuda()
         grey = torch.from_numpy(host_frames[0]).cuda()
+        q0 = torch.from_numpy(np.resize(fq[0]["corners"], (nq, 4, 2)).astype(np.float32)).cuda()
         with torch.cuda.stream(stream):
             for _ in range(args.warmup):
-                dec = decode.decode_quads(grey, quads_c, fam, stream=stream)
+                dec = decode.decode_quads(grey, q0, fam, stream=stream)
             a.record(stream)
             for _ in range(args.steps):
-                dec = decode.decode_quads(grey, quads_c, fam, stream=stream)
+                dec = decode.decode_quads(grey, q0, fam, stream=stream)
             b.record(stream)
         b.synchronize()
         dms = a.elapsed_time(b) / args.steps
@@ -528,17 +667,36 @@ def main():
         decode_line = {"quads": nq, "family_codes": 587, "ms": dms, "quads_per_s": nq / (dms / 1000.0),
                        "read": int((dn["status"] == 0).sum())}
 
-    # --- serving: 8 cameras (4 x 720p60, 4 x 1080p30), Poisson arrivals
+    # --- serving: 8 cameras (4 x 720p60, 4 x 1080p30), Poisson arrivals;
+    # then the same cameras at 16x their rates (more requests than one
+    # launch per request keeps up with: they batch), and bursts of 16
+    # simultaneous requests
     serving_line = None
     if cam_frames:
         from atag import serving
         slots = serving.executors_for_memory(W, H, 8, 8 * W * H, max_slots=3)
-        srv = serving.Server(slots)
         rates = [60.0] * 4 + [30.0] * 4
-        res = serving.run_cameras(srv, cam_frames, rates, duration_s=args.serving_seconds, seed=1)
+
+        def run(fn, **kw):
+            srv = serving.Server(slots)
+            serving.warm(srv, cam_frames[4][0])
+            res = fn(srv, cam_frames, **kw)
+            return srv, res
+        srv, res = run(serving.run_cameras, rates_hz=rates, duration_s=args.serving_seconds, seed=1)
         serving_line = serving.latency_summary(res, args.serving_seconds)
-        serving_line["cameras"] = "4x1280x720@60 + 4x1920x1080@30"
-        serving_line["slots"] = len(slots)
+        serving_line.update({"cameras": "4x1280x720@60 + 4x1920x1080@30", "slots": len(slots),
+                             "seconds": args.serving_seconds, "max_in_flight": srv.max_in_flight})
+        if args.overload_seconds > 0:
+            srv, res = run(serving.run_cameras, rates_hz=[16 * r for r in rates], duration_s=args.overload_seconds,
+                           seed=2)
+            ov = serving.latency_summary(res, args.overload_seconds)
+            ov.update({"cameras": "4x1280x720@960 + 4x1920x1080@480", "seconds": args.overload_seconds,
+                       "max_in_flight": srv.max_in_flight})
+            serving_line["overload_16x"] = ov
+            srv, res = run(serving.run_bursts, n_bursts=100, burst_size=16, period_s=0.02)
+            bu = serving.latency_summary(res, 2.0)
+            bu.update({"bursts": "100 bursts of 16 requests, one every 20 ms", "max_in_flight": srv.max_in_flight})
+            serving_line["bursts_16"] = bu
         del slots, srv
 
     # --- CPU baseline (rank 0, N=1)
@@ -561,6 +719,27 @@ def main():
         cpu = {"value": passes * len(sample) / cdt, "unit": "frames/s", "cores": used, "kind": "port",
                "sample": f"{passes} passes over {len(sample)} synthetic 1920x1080 frames (the batch's first "
                          f"frames), OpenMP over frames, {cdt:.1f} s"}
+        if vga_frames:
+            # the reference's CPU-path configuration: 640x480 at decimate 2,
+            # one frame at a time on one thread (latency), then all threads
+            vcfg = oracle.default_config(decimate=2)
+            oracle.detect_many(vga_frames[:1], vcfg, threads=1)
+            lat = []
+            for f in vga_frames:
+                t0 = time.perf_counter()
+                oracle.detect_many([f], vcfg, threads=1)
+                lat.append(1000.0 * (time.perf_counter() - t0))
+            lat.sort()
+            t0 = time.perf_counter()
+            reps = 0
+            while time.perf_counter() - t0 < 2.0:
+                _, vused = oracle.detect_many(vga_frames, vcfg, threads=0)
+                reps += 1
+            vdt = time.perf_counter() - t0
+            cpu["vga_d2"] = {"frames_per_s_1_thread": 1000.0 * len(lat) / sum(lat), "p50_ms": lat[len(lat) // 2],
+                             "p99_ms": lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))],
+                             "frames_per_s_all_threads": reps * len(vga_frames) / vdt, "threads": vused,
+                             "sample": f"{len(vga_frames)} synthetic 640x480 frames (8 tags), decimate 2"}
 
     nq = [int(s["n_quads"]) for s in stats]
     line = {
@@ -575,6 +754,7 @@ def main():
         "plain": plain,
         "batched_vs_plain": value / world / plain["frames_per_s"] if plain else None,
         "mixed_batch": mixed,
+        "configs": configs,
         "refine": refine_line,
         "pose": pose_line,
         "decode": decode_line,
