@@ -554,44 +554,80 @@ atag_status atag_estimate_pose(const float *d_corners, size_t corner_stride, siz
                                atag_pose *d_poses, atag_stream_t stream);
 
 /* ------------------------------------------------------------------ */
-/* Reading tags: the bit grid of each quad against a code family.       */
-/* The reference passes each quad to the AprilTag library's             */
-/* quad_decode_task with tag36h11 (src/quad_decoding.cpp:46-128); that  */
-/* library and its family tables are not in the reference tree, so the */
-/* family's codes are an argument.                                      */
+/* Reading tags: each quad's bits against a code family.  The reference */
+/* hands each quad to the AprilTag library's quad_decode_task with       */
+/* tag36h11 and the detector defaults plus quad_decimate = 1            */
+/* (src/quad_decoding.cpp:46-75); that library and its family tables    */
+/* are not in the reference tree, so the family is an argument, in the  */
+/* library's own terms.                                                  */
 /* ------------------------------------------------------------------ */
 #define ATAG_DECODE_REORDERED 0x1u    /* corners were wound the other way        */
-#define ATAG_DECODE_DEGENERATE 0x2u   /* the corners admit no homography         */
-#define ATAG_DECODE_LOW_CONTRAST 0x4u /* white ring minus black border below
-                                         min_contrast: no bits read               */
+#define ATAG_DECODE_DEGENERATE 0x2u   /* no homography, or part of the tag
+                                         projects behind the camera            */
+#define ATAG_DECODE_LOW_CONTRAST 0x4u /* white minus black grey model at the tag
+                                         centre below min_contrast, or a model
+                                         without enough samples: no bits read  */
+
+/* A tag family as the AprilTag library describes one: bit i of a code
+ * (code bit nbits - 1 - i) is the cell (bit_x[i], bit_y[i]) of a grid whose
+ * cells 0 .. width_at_border - 1 span the outer edge of the black border
+ * (cells may lie outside it: coordinates are signed); total_width cells
+ * span the whole tag (the sharpening grid, at most 16).  The layout must
+ * carry bit cells onto bit cells under quarter turns, as the library's
+ * families do.  A code with bits at or above nbits never matches. */
+typedef struct atag_tag_family {
+    uint32_t nbits;           /* 1..64                                          */
+    uint32_t width_at_border; /* at least 3                                     */
+    uint32_t total_width;     /* total_width - width_at_border even             */
+    uint32_t reversed_border; /* 1: the border is white on black                */
+    const int8_t *h_bit_x;    /* host arrays of nbits cell coordinates          */
+    const int8_t *h_bit_y;
+    const uint64_t *d_codes;  /* device array of n_codes codes                  */
+    uint32_t n_codes;
+    uint32_t max_hamming;     /* largest accepted distance (bits corrected)     */
+} atag_tag_family;
+
+/* The library's detector parameters that decoding reads. */
+typedef struct atag_decode_params {
+    float decode_sharpening;  /* 0.25                                           */
+    int32_t refine_edges;     /* 1: refine each edge before reading             */
+    int32_t quad_decimate;    /* 1: edge search +-(quad_decimate + 1) px        */
+    float min_contrast;       /* 0: reject when the white model is not brighter */
+} atag_decode_params;
+void atag_decode_params_default(atag_decode_params *params);
+
 typedef struct atag_decoded {
-    uint64_t code;      /* bits read, cell (r, c) at bit D*D-1-(D r + c), rotation 0 */
-    int32_t id;         /* index of the matched code, -1 if none within max_hamming */
-    uint32_t hamming;   /* distance to the nearest code over the four rotations     */
-    uint32_t rotation;  /* quarter turns of the read grid that give the match       */
-    uint32_t status;    /* ATAG_DECODE_* bits                                       */
-    float black, white; /* mean grey of the black border and of the ring outside it */
-    float margin;       /* smallest |sample - threshold| over the data cells        */
+    uint64_t code;           /* bits read, before any rotation (bit nbits-1-i = bit i) */
+    int32_t id;              /* index of the matched code, -1 if none            */
+    uint32_t hamming;        /* distance to the nearest code over the 4 turns    */
+    uint32_t rotation;       /* quarter turns of the read grid that give the match */
+    uint32_t status;         /* ATAG_DECODE_* bits                               */
+    float decision_margin;   /* min(mean value of white bits, mean magnitude of
+                                black bits), after sharpening                    */
+    float black, white;      /* grey models at the tag centre                    */
+    float corners[4][2];     /* the edge-refined corners; for a match, turned so
+                                that corner 0 is the tag's first corner          */
     uint32_t reserved;
 } atag_decoded;
 
-/* Tag layout: data_side x data_side data cells (2..8) inside a one-cell
- * black border inside a white quiet zone; the quad is the outer edge of the
- * black border, its corners as for atag_estimate_pose (a quad wound the
- * other way is read mirrored back and flagged).  Per quad: the projective
- * map of the unit square onto the quad in closed form, bilinear samples at
- * cell centres (pixel centres at integer coordinates), threshold halfway
- * between the mean of the black border cells and the mean of the ring of
- * cells just outside it, bit = sample > threshold; then the code of d_codes
- * (n_codes 64-bit codes, bit D*D-1-(D r + c) = cell r, c) and quarter turn
- * with the smallest Hamming distance (first on ties), accepted at most
- * max_hamming.  corner_stride as for atag_estimate_pose (40: detector
- * output); pitch 0 = width. */
+/* Per quad (corners as for atag_estimate_pose, used as given, as the
+ * reference passes its QuadCorners to the library): a quad wound the other
+ * way is read with corners 0, 3, 2, 1 and flagged; the edges are refined
+ * (params->refine_edges); the homography of the tag square [-1, 1]^2 onto
+ * the quad; planar grey models (least squares) of the white ring just
+ * outside the black border and of the border, from nearest-pixel samples
+ * one per cell along each side; each bit's bilinear sample (pixel centres
+ * at +0.5) minus the models' mean, sharpened by decode_sharpening times the
+ * 4-neighbour Laplacian of the bit grid, bit = value > 0; the decision
+ * margin; the code and quarter turn with the smallest Hamming distance
+ * (ties: fewer turns, then the lower index), accepted at most max_hamming
+ * with a decision margin of at least 0.  params may be NULL (defaults).
+ * corner_stride: 40 for detector output, 32 for packed corners; pitch 0 =
+ * width. */
 atag_status atag_decode_quads(const uint8_t *d_image, size_t width, size_t height, size_t pitch,
                               const float *d_corners, size_t corner_stride, size_t n_quads,
-                              const uint64_t *d_codes, size_t n_codes, uint32_t data_side,
-                              uint32_t max_hamming, double min_contrast, atag_decoded *d_out,
-                              atag_stream_t stream);
+                              const atag_tag_family *family, const atag_decode_params *params,
+                              atag_decoded *d_out, atag_stream_t stream);
 
 /* Launch shapes of the detector's kernels.  Every choice gives the same
  * results; only the speed changes.  atag_detector_create starts from the

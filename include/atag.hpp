@@ -154,15 +154,15 @@ inline atag_status estimate_pose(cudaStream_t q, const float* corners, size_t co
                               as_stream(q));
 }
 
-// Reads each quad's bit grid and matches it against a code family (the
-// reference's decode_quads, src/quad_decoding.cpp:84-128, with the family
-// as an argument).
+// Reads each quad's bits against a tag family described as the AprilTag
+// library describes its families (the reference's decode_quads,
+// src/quad_decoding.cpp:84-128, with the family as an argument).
 inline atag_status decode_quads(cudaStream_t q, const uint8_t* image, size_t width, size_t height,
-                                const float* corners, size_t corner_stride, size_t n_quads, const uint64_t* codes,
-                                size_t n_codes, uint32_t data_side, uint32_t max_hamming, atag_decoded* out,
-                                double min_contrast = 10.0, size_t pitch = 0) {
-    return atag_decode_quads(image, width, height, pitch, corners, corner_stride, n_quads, codes, n_codes, data_side,
-                             max_hamming, min_contrast, out, as_stream(q));
+                                const float* corners, size_t corner_stride, size_t n_quads,
+                                const atag_tag_family& family, atag_decoded* out,
+                                const atag_decode_params* params = nullptr, size_t pitch = 0) {
+    return atag_decode_quads(image, width, height, pitch, corners, corner_stride, n_quads, &family, params, out,
+                             as_stream(q));
 }
 
 // RAII owner of an atag_detector (the whole path of src/main.cpp:322-1024).

@@ -7,7 +7,8 @@ import ctypes
 import os
 import re
 
-from .records import ClusterOutputs, ClusterPointC, Config, Frame, FrameViews, LineFitPointC, Limits, Tuning
+from .records import (ClusterOutputs, ClusterPointC, Config, DecodeParams, Frame, FrameViews, LineFitPointC,
+                      Limits, TagFamily, Tuning)
 
 PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG_ROOT, "lib", "libatag_gb300.so")
@@ -65,7 +66,9 @@ _SIGNATURES = {
     "atag_refine_forward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P]),
     "atag_refine_backward": (_ST, [_P, _SZ, _SZ, _P, _SZ, _P, _P, _P, _P, _P, _P]),
     "atag_estimate_pose": (_ST, [_P, _SZ, _SZ, _D, _D, _D, _D, _D, _U32, _P, _P]),
-    "atag_decode_quads": (_ST, [_P, _SZ, _SZ, _SZ, _P, _SZ, _SZ, _P, _SZ, _U32, _U32, _D, _P, _P]),
+    "atag_decode_quads": (_ST, [_P, _SZ, _SZ, _SZ, _P, _SZ, _SZ, ctypes.POINTER(TagFamily),
+                                ctypes.POINTER(DecodeParams), _P, _P]),
+    "atag_decode_params_default": (None, [ctypes.POINTER(DecodeParams)]),
 }
 STAGE_COUNT = 16
 

@@ -27,9 +27,10 @@ POSE = np.dtype([("R", "<f8", (3, 3)), ("t", "<f8", (3,)), ("H", "<f8", (3, 3)),
                  ("iterations", "<u4"), ("status", "<u4")])
 
 DECODED = np.dtype([("code", "<u8"), ("id", "<i4"), ("hamming", "<u4"), ("rotation", "<u4"), ("status", "<u4"),
-                    ("black", "<f4"), ("white", "<f4"), ("margin", "<f4"), ("reserved", "<u4")])
+                    ("decision_margin", "<f4"), ("black", "<f4"), ("white", "<f4"), ("corners", "<f4", (4, 2)),
+                    ("reserved", "<u4")])
 
-assert POSE.itemsize == 184 and DECODED.itemsize == 40
+assert POSE.itemsize == 184 and DECODED.itemsize == 72
 assert BOUNDARY_POINT.itemsize == 4 and CLUSTER_POINT.itemsize == 8 and CLUSTER_EXTENTS.itemsize == 8
 assert CLUSTER_BOUNDS.itemsize == 32 and LINE_FIT_POINT.itemsize == 64 and CORNER.itemsize == 12
 assert FITTED_QUAD.itemsize == 272 and QUAD_CORNERS.itemsize == 40 and FRAME_STATS.itemsize == 64
@@ -99,6 +100,19 @@ class ClusterOutputs(ctypes.Structure):
                 ("cluster_points", ctypes.c_void_p), ("cluster_indices", ctypes.c_void_p),
                 ("line_fit_points", ctypes.c_void_p), ("point_capacity", ctypes.c_size_t),
                 ("counts", ctypes.c_void_p)]
+
+
+class TagFamily(ctypes.Structure):
+    """atag_tag_family (bit cells on the host, codes on the device)."""
+    _fields_ = [("nbits", ctypes.c_uint32), ("width_at_border", ctypes.c_uint32), ("total_width", ctypes.c_uint32),
+                ("reversed_border", ctypes.c_uint32), ("h_bit_x", ctypes.c_void_p), ("h_bit_y", ctypes.c_void_p),
+                ("d_codes", ctypes.c_void_p), ("n_codes", ctypes.c_uint32), ("max_hamming", ctypes.c_uint32)]
+
+
+class DecodeParams(ctypes.Structure):
+    """atag_decode_params."""
+    _fields_ = [("decode_sharpening", ctypes.c_float), ("refine_edges", ctypes.c_int32),
+                ("quad_decimate", ctypes.c_int32), ("min_contrast", ctypes.c_float)]
 
 
 class Tuning(ctypes.Structure):

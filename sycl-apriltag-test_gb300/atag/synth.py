@@ -199,3 +199,160 @@ def batch_specs(n: int, seed: int):
         specs.append(FrameSpec(w, h, int(rng.integers(0, 61)), (16, 300), int(rng.integers(0, 1001)),
                                (0.5, 1.5), (2.0, 8.0)))
     return specs
+
+
+# ---------------------------------------------------------------------------
+# Tag families for reading tags.  A family is described the way the
+# AprilTag library describes one: nbits data bits, bit i in the cell
+# (bit_x[i], bit_y[i]) of a grid in which cells 0 .. width_at_border - 1
+# span the outer edge of the black border, total_width cells across the
+# whole tag (white quiet zone included), and codes whose bit nbits - 1 - i
+# holds bit i.  The code tables of the library's families are not
+# reproduced here; these are seeded stand-ins with the same geometry.
+# ---------------------------------------------------------------------------
+@dataclass
+class TagLayout:
+    bit_x: tuple
+    bit_y: tuple
+    width_at_border: int
+    total_width: int
+
+    @property
+    def nbits(self):
+        return len(self.bit_x)
+
+    def rotation_perm(self):
+        """perm[i] = j: after one quarter turn of the read grid, bit i holds
+        what bit j held (cell (x, y) takes the content of cell
+        (W - 1 - y, x))."""
+        W = self.width_at_border
+        where = {(x, y): j for j, (x, y) in enumerate(zip(self.bit_x, self.bit_y))}
+        return [where[(W - 1 - y, x)] for x, y in zip(self.bit_x, self.bit_y)]
+
+    def rotate(self, code, turns=1):
+        n, perm = self.nbits, self.rotation_perm()
+        for _ in range(turns % 4):
+            out = 0
+            for i, j in enumerate(perm):
+                if (code >> (n - 1 - j)) & 1:
+                    out |= 1 << (n - 1 - i)
+            code = out
+        return code
+
+    def cells(self, code):
+        """total_width x total_width grid of the rendered tag (True = white):
+        quiet zone white, border ring black, data cells from the code, other
+        inner cells white."""
+        W, T = self.width_at_border, self.total_width
+        m = (W - T) // 2  # grid coordinate of cell 0
+        g = np.ones((T, T), bool)
+        for y in range(T):
+            for x in range(T):
+                bx, by = x + m, y + m
+                if 0 <= bx < W and 0 <= by < W and (bx in (0, W - 1) or by in (0, W - 1)):
+                    g[y, x] = False
+        n = self.nbits
+        for i, (bx, by) in enumerate(zip(self.bit_x, self.bit_y)):
+            g[by - m, bx - m] = bool((code >> (n - 1 - i)) & 1)
+        return g
+
+
+def classic_layout(D=6):
+    """D x D data bits in row-major order inside a one-cell black border and
+    a one-cell white quiet zone (width_at_border D + 2, total_width D + 4)."""
+    return TagLayout(tuple(1 + i % D for i in range(D * D)), tuple(1 + i // D for i in range(D * D)), D + 2, D + 4)
+
+
+def quadrant_layout(D=6):
+    """The same cells as classic_layout, with the bits ordered the way the
+    AprilTag 3 families order theirs: a quarter of the bits, then the same
+    cells turned by one, two and three quarter turns, so that turning the
+    tag shifts the code by nbits / 4 bits."""
+    assert D % 2 == 0
+    W = D + 2
+    # one cell of every orbit under quarter turns, in row-major order
+    quarter = []
+    seen = set()
+    for x, y in [(1 + c, 1 + r) for r in range(D) for c in range(D)]:
+        orbit = [(x, y)]
+        for _ in range(3):
+            px, py = orbit[-1]
+            orbit.append((W - 1 - py, px))
+        if not seen.intersection(orbit):
+            quarter.append((x, y))
+            seen.update(orbit)
+    cells = []
+    for k in range(4):
+        for x, y in quarter:
+            for _ in range(k):
+                x, y = y, W - 1 - x  # the cell whose content one quarter turn brings here
+            cells.append((x, y))
+    return TagLayout(tuple(c[0] for c in cells), tuple(c[1] for c in cells), W, D + 4)
+
+
+def random_family(layout: TagLayout, n: int, seed: int, min_distance: int = 8):
+    """n seeded codes whose distances to each other over all quarter turns,
+    and to their own turns, are at least min_distance."""
+    rng = np.random.default_rng(seed)
+    nb = layout.nbits
+    codes = []
+    while len(codes) < n:
+        c = int(rng.integers(0, 1 << nb, dtype=np.uint64)) if nb < 64 else int(rng.integers(0, 1 << 63)) * 2
+        rots = [c] + [layout.rotate(c, k) for k in (1, 2, 3)]
+        if any(bin(c ^ r).count("1") < min_distance for r in rots[1:]):
+            continue
+        if any(bin(r ^ o).count("1") < min_distance for r in rots for o in codes):
+            continue
+        codes.append(c)
+    return codes
+
+
+def _render_cells(img, quad, grid):
+    """Paints a T x T cell grid (True = white) onto the image through the
+    homography that maps the grid square onto `quad`."""
+    h, w = img.shape
+    T = grid.shape[0]
+    H = _homography(quad, np.array([[0, 0], [T, 0], [T, T], [0, T]], np.float64))
+    x0 = int(max(0, np.floor(quad[:, 0].min())))
+    x1 = int(min(w - 1, np.ceil(quad[:, 0].max())))
+    y0 = int(max(0, np.floor(quad[:, 1].min())))
+    y1 = int(min(h - 1, np.ceil(quad[:, 1].max())))
+    if x1 <= x0 or y1 <= y0:
+        return
+    ys, xs = np.mgrid[y0:y1 + 1, x0:x1 + 1]
+    X, Y = xs + 0.5, ys + 0.5
+    d = H[2, 0] * X + H[2, 1] * Y + H[2, 2]
+    u = (H[0, 0] * X + H[0, 1] * Y + H[0, 2]) / d
+    v = (H[1, 0] * X + H[1, 1] * Y + H[1, 2]) / d
+    inside = (u >= 0) & (u < T) & (v >= 0) & (v < T)
+    val = np.where(grid[np.clip(v.astype(np.int64), 0, T - 1), np.clip(u.astype(np.int64), 0, T - 1)], 255, 0)
+    sub = img[y0:y1 + 1, x0:x1 + 1]
+    sub[inside] = val[inside].astype(np.float32)
+
+
+def family_frame(seed: int, layout: TagLayout, codes, n_tags: int = 12, width: int = 1280, height: int = 720,
+                 blur: float = 0.6, noise: float = 2.0, max_tilt_deg: float = 30.0):
+    """A frame of n_tags tags of a family on a noisy grey background.
+    Returns the uint8 image and, per tag, (code index, the outer corners of
+    its black border with pixel centres at integer coordinates, in the order
+    that reads the tag unturned)."""
+    rng = np.random.default_rng(seed)
+    img = rng.uniform(100, 160, size=(height, width)).astype(np.float32)
+    T, W = layout.total_width, layout.width_at_border
+    m = (T - W) // 2
+    tags, boxes = [], []
+    while len(tags) < n_tags:
+        side = rng.uniform(60, 160)
+        cx, cy = rng.uniform(side, width - side), rng.uniform(side, height - side)
+        if any(abs(cx - bx) < (side + bs) * 0.75 and abs(cy - by) < (side + bs) * 0.75 for bx, by, bs in boxes):
+            continue
+        boxes.append((cx, cy, side))
+        quad = _tag_quad(rng, cx, cy, side, max_tilt_deg)
+        k = int(rng.integers(0, len(codes)))
+        _render_cells(img, quad, layout.cells(codes[k]))
+        H = _homography(np.array([[0, 0], [T, 0], [T, T], [0, T]], np.float64), quad)
+        inner = np.array([[m, m, 1], [m + W, m, 1], [m + W, m + W, 1], [m, m + W, 1]], np.float64)
+        p = inner @ H.T
+        tags.append((k, p[:, :2] / p[:, 2:] - 0.5))
+    img = _blur(img, blur) + rng.normal(0, noise, size=img.shape).astype(np.float32)
+    return np.clip(np.rint(img), 0, 255).astype(np.uint8), tags

@@ -53,34 +53,3 @@ def small_frames():
     sq[45:75, 65:95] = 230
     out["square"] = sq
     return out
-
-
-def family_frame(seed: int, codes, n_tags: int = 12, width: int = 1280, height: int = 720, blur: float = 0.6,
-                 noise: float = 2.0):
-    """A frame with n_tags tags of the given code family (10 x 10 cells:
-    white quiet zone, black border, 6 x 6 data bits) on a noisy grey
-    background.  Returns the uint8 image and, per tag, (code index, the
-    corners of the black border's outer edge with pixel centres at integer
-    coordinates)."""
-    import numpy as np
-    from atag import synth
-    from decode_ref import code_bits
-    rng = np.random.default_rng(seed)
-    img = rng.uniform(100, 160, size=(height, width)).astype(np.float32)
-    tags, boxes = [], []
-    while len(tags) < n_tags:
-        side = rng.uniform(60, 160)
-        cx, cy = rng.uniform(side, width - side), rng.uniform(side, height - side)
-        if any(abs(cx - bx) < (side + bs) * 0.75 and abs(cy - by) < (side + bs) * 0.75 for bx, by, bs in boxes):
-            continue
-        boxes.append((cx, cy, side))
-        quad = synth._tag_quad(rng, cx, cy, side, 30.0)  # the 10-cell square, pixel centres at +0.5
-        k = int(rng.integers(0, len(codes)))
-        synth._render_tag(img, rng, quad, code_bits(codes[k]))
-        # the black border's outer edge is cells 1..9 of the 10-cell square
-        H = synth._homography(np.array([[0, 0], [10, 0], [10, 10], [0, 10]], np.float64), quad)
-        inner = np.array([[1, 1], [9, 1], [9, 9], [1, 9]], np.float64)
-        p = np.c_[inner, np.ones(4)] @ H.T
-        tags.append((k, p[:, :2] / p[:, 2:] - 0.5))
-    img = synth._blur(img, blur) + rng.normal(0, noise, size=img.shape).astype(np.float32)
-    return np.clip(np.rint(img), 0, 255).astype(np.uint8), tags

@@ -93,7 +93,7 @@ def test_calls_without_device_return_status(monkeypatch):
     st = L.atag_estimate_pose(None, 32, 4, 1000.0, 1000.0, 960.0, 540.0, 0.16, 20, None, None)
     assert st == 5
     assert L.atag_refine_forward(None, 64, 64, None, 1, None, None, None, None) == 5
-    assert L.atag_decode_quads(None, 64, 64, 64, None, 32, 1, None, 0, 6, 2, 10.0, None, None) == 5
+    assert L.atag_decode_quads(None, 64, 64, 64, None, 32, 1, None, None, None, None) == 5
     assert L.atag_cluster(None, None, None, 64, 64, None, 0, None, None) == 5
     assert L.atag_corner_peaks(None, None, 1, None, 0, None, 0, None, 0, None, None) == 5
 
