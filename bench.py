@@ -708,13 +708,14 @@ def main():
         srv, res = run(serving.run_cameras, rates_hz=rates, duration_s=args.serving_seconds, seed=1)
         serving_line = serving.latency_summary(res, args.serving_seconds)
         serving_line.update({"cameras": "4x1280x720@60 + 4x1920x1080@30", "slots": len(slots),
-                             "seconds": args.serving_seconds, "max_in_flight": srv.max_in_flight})
+                             "seconds": args.serving_seconds, "max_in_flight": srv.max_in_flight,
+                             "max_host_stall_ms": 1000.0 * srv.max_poll_gap})
         if args.overload_seconds > 0:
             srv, res = run(serving.run_cameras, rates_hz=[16 * r for r in rates], duration_s=args.overload_seconds,
                            seed=2)
             ov = serving.latency_summary(res, args.overload_seconds)
             ov.update({"cameras": "4x1280x720@960 + 4x1920x1080@480", "seconds": args.overload_seconds,
-                       "max_in_flight": srv.max_in_flight})
+                       "max_in_flight": srv.max_in_flight, "max_host_stall_ms": 1000.0 * srv.max_poll_gap})
             serving_line["overload_16x"] = ov
             srv, res = run(serving.run_bursts, n_bursts=100, burst_size=16, period_s=0.02)
             bu = serving.latency_summary(res, 2.0)

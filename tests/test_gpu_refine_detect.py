@@ -10,22 +10,31 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
-def match_errors(quads, truth, gate=3.0):
-    """Per matched quad: the largest corner distance to its true quad (over
-    the corner order and winding that fit best); quads farther than `gate`
-    px from every true quad (clutter, covered tags) are left out."""
-    out = []
-    for q in quads:
-        c = q["corners"].astype(np.float64)
-        best = None
-        for t in truth:
-            for order in (t, t[::-1]):
-                for k in range(4):
-                    d = np.linalg.norm(np.roll(order, k, axis=0) - c, axis=1).max()
-                    best = d if best is None or d < best else best
-        if best is not None and best < gate:
-            out.append(best)
-    return np.array(out)
+def best_truth(c, truth):
+    """(largest corner distance, true corners in the matching order) of the
+    true quad closest to corners c, over corner order and winding."""
+    best = (np.inf, None)
+    for t in truth:
+        for order in (t, t[::-1]):
+            for k in range(4):
+                o = np.roll(order, k, axis=0)
+                d = np.linalg.norm(o - c, axis=1).max()
+                if d < best[0]:
+                    best = (d, o)
+    return best
+
+
+def paired_errors(q0, q1, truth, gate=3.0):
+    """For each unrefined quad within `gate` px of a tag (not clutter or a
+    covered tag): its largest corner error and that of the same quad
+    refined, against the same true corners."""
+    e0, e1 = [], []
+    for a, b in zip(q0, q1):
+        d, t = best_truth(a["corners"].astype(np.float64), truth)
+        if d < gate:
+            e0.append(d)
+            e1.append(np.linalg.norm(b["corners"].astype(np.float64) - t, axis=1).max())
+    return np.array(e0), np.array(e1)
 
 
 def test_refined_corners_are_closer_to_truth():
@@ -44,15 +53,16 @@ def test_refined_corners_are_closer_to_truth():
         assert s0.tobytes() == s1.tobytes()
         assert len(q0[0]) == len(q1[0])
         assert np.array_equal(q0[0]["blob_index"], q1[0]["blob_index"])
-        m0, m1 = match_errors(q0[0], truth), match_errors(q1[0], truth)
-        assert len(m0) >= 10 and len(m1) == len(m0)
+        m0, m1 = paired_errors(q0[0], q1[0], truth)
+        assert len(m0) >= 10
         e0.append(m0)
         e1.append(m1)
     e0, e1 = np.concatenate(e0), np.concatenate(e1)
-    print(f"max corner error per quad vs truth: unrefined mean {e0.mean():.3f} px, median {np.median(e0):.3f}; "
-          f"refined mean {e1.mean():.3f} px, median {np.median(e1):.3f} ({len(e0)} quads)")
-    assert e1.mean() < 0.75 * e0.mean()
-    assert np.median(e1) < np.median(e0)
+    print(f"largest corner error per quad vs truth ({len(e0)} quads): unrefined median {np.median(e0):.3f} px, "
+          f"mean {e0.mean():.3f}; refined median {np.median(e1):.3f} px, mean {e1.mean():.3f}; "
+          f"refined closer for {np.mean(e1 < e0):.0%}")
+    assert np.median(e1) < 0.75 * np.median(e0)
+    assert np.mean(e1 < e0) > 0.8
 
 
 def test_refinement_stage_equals_refine_forward():
@@ -68,7 +78,8 @@ def test_refinement_stage_equals_refine_forward():
     det.set_refinement(True)
     q1, _ = det.detect([t])
     corners = torch.from_numpy(q0[0]["corners"].copy()).cuda()
-    r, _, _ = refine.refine_forward(t.float().div(255.0), corners)
+    # value / 255 with IEEE division (numpy), as the stage reads the u8 frame
+    r, _, _ = refine.refine_forward(torch.from_numpy(img.astype(np.float32) / np.float32(255.0)).cuda(), corners)
     want = r.cpu().numpy()
     got = q1[0]["corners"]
     same = (got == want).all(axis=2)
