@@ -699,6 +699,8 @@ def main():
         from atag import serving
         slots = serving.executors_for_memory(W, H, 8, 8 * W * H, max_slots=3)
         rates = [60.0] * 4 + [30.0] * 4
+        # the cameras deliver into pinned capture buffers (no host-side copy)
+        cam_frames = [[torch.from_numpy(f).pin_memory() for f in fr] for fr in cam_frames]
 
         def run(fn, **kw):
             srv = serving.Server(slots)

@@ -28,8 +28,14 @@ import numpy as np
 class Request:
     seq: int
     camera: int
-    frame: np.ndarray          # H x W uint8, source resolution
+    frame: object              # H x W uint8, source resolution: a numpy array, or a
+                               # pinned host tensor (a capture buffer) copied to the
+                               # device without a host-side copy
     t_arrival: float           # seconds, on the server clock
+
+
+def frame_pixels(frame) -> int:
+    return int(frame.shape[0]) * int(frame.shape[1])
 
 
 @dataclass
@@ -76,13 +82,17 @@ class DetectorExecutor:
         torch = self.torch
         off = 0
         views = []
-        for f in frames:
-            n = f.size
-            self.h_in[off:off + n].numpy()[:] = f.reshape(-1)
-            views.append((off, f.shape))
-            off += n
         with torch.cuda.stream(self.stream):
-            self.d_in[:off].copy_(self.h_in[:off], non_blocking=True)
+            for f in frames:
+                n = frame_pixels(f)
+                if isinstance(f, torch.Tensor) and f.is_pinned():
+                    # a capture buffer in pinned memory: straight to the device
+                    self.d_in[off:off + n].copy_(f.reshape(-1), non_blocking=True)
+                else:
+                    self.h_in[off:off + n].numpy()[:] = np.asarray(f).reshape(-1)
+                    self.d_in[off:off + n].copy_(self.h_in[off:off + n], non_blocking=True)
+                views.append((off, tuple(f.shape)))
+                off += n
             dev = [self.d_in[o:o + s[0] * s[1]].view(s[0], s[1]) for o, s in views]
             self.det.enqueue(dev, stream=self.stream)
             self.h_stats.copy_(self.det.d_stats, non_blocking=True)
@@ -163,10 +173,10 @@ class Server:
                 continue
             max_frames, max_pixels = ex.capacity()
             take, px = [], 0
-            while self.queue and len(take) < max_frames and px + self.queue[0].frame.size <= max_pixels:
+            while self.queue and len(take) < max_frames and px + frame_pixels(self.queue[0].frame) <= max_pixels:
                 r = self.queue.popleft()
                 take.append(r)
-                px += r.frame.size
+                px += frame_pixels(r.frame)
             if not take:  # a single frame larger than the slot's budget
                 raise ValueError("frame exceeds the slot pixel budget")
             ex.launch([r.frame for r in take])

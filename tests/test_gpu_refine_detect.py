@@ -66,8 +66,8 @@ def test_refined_corners_are_closer_to_truth():
 
 
 def test_refinement_stage_equals_refine_forward():
-    """The in-detector stage gives atag_refine_forward's corners on the
-    frame's FP32-normalised grey image."""
+    """The in-detector stage gives atag_refine_forward's corners (within
+    1e-3 px) on the frame's FP32-normalised grey image."""
     from atag import refine, synth
     from atag.detector import Detector
     img = synth.render(synth.CONFIGS["1080p"], 711)
@@ -82,7 +82,8 @@ def test_refinement_stage_equals_refine_forward():
     r, _, _ = refine.refine_forward(torch.from_numpy(img.astype(np.float32) / np.float32(255.0)).cuda(), corners)
     want = r.cpu().numpy()
     got = q1[0]["corners"]
-    same = (got == want).all(axis=2)
+    # the same arithmetic in two instantiations; FMA contraction may differ
+    same = (np.abs(got - want) < 1e-3).all(axis=2)
     kept = (got == q0[0]["corners"]).all(axis=2)  # nearly parallel edge lines
     assert np.all(same | kept)
     assert same.mean() > 0.95

@@ -91,10 +91,12 @@ def test_overloaded_cameras_are_batched():
     from atag import serving
     cams = _cameras()
     alone = _alone(cams)
+    # the cameras deliver into pinned capture buffers
+    pinned = [[torch.from_numpy(f).pin_memory() for f in fr] for fr in cams]
     slots = serving.executors_for_memory(1920, 1080, 8, 8 * 1920 * 1080, max_slots=3)
     srv = serving.Server(slots)
-    serving.warm(srv, cams[4][0])
-    res = serving.run_cameras(srv, cams, [960.0] * 4 + [480.0] * 4, duration_s=1.0, seed=9)
+    serving.warm(srv, pinned[4][0])
+    res = serving.run_cameras(srv, pinned, [960.0] * 4 + [480.0] * 4, duration_s=1.0, seed=9)
     assert len(res) > 4000
     assert srv.max_in_flight >= 2
     assert max(r.batch_size for r in res) > 1
