@@ -67,13 +67,6 @@ struct FrameDesc {
     // DEAD_PAIRS keys (EMPTY = ~0) of pairs whose running point count is
     // already above the cluster size limit; null when not tracked
     unsigned long long* dead_pairs;
-    // One bit per 2x2 block and colour, written by the tile CCL: the block's
-    // component (its 255-slot, its 0-slot) has at least big_min pixels inside
-    // the block's CCL tile, so at least that many in all and the size test
-    // of the boundary points needs no gather.  Per block row, (w/2 + 31)/32
-    // pairs of words (255-forest, 0-forest); null when not kept.
-    uint32_t* bigmap;
-    uint32_t big_min;
     // iteration cap of the frame-wide union-find loops (0: the bound the
     // tile count gives, see k_pixels.cu)
     uint32_t uf_cap;

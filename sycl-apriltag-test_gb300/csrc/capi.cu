@@ -194,7 +194,6 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, bool ow
     f.cluster_runs = (uint32_t*)take(4ull * c.cluster_cap);
     f.counters = (uint32_t*)take(4ull * CNT_COUNT);
     f.dead_pairs = (unsigned long long*)take(8ull * DEAD_PAIRS);
-    f.bigmap = (uint32_t*)take(8ull * (h / 2) * ((w / 2 + 31) / 32));
     if (d) *d = f;
     return off;
 }
@@ -1031,7 +1030,6 @@ atag_status atag_detect_batch(atag_detector* det, const atag_frame* frames, size
         d.quad_cap = (uint32_t)quad_cap;
         d.stats = d_stats + i;
         d.stage_outputs = det->keep_intermediates ? 1u : 0u;
-        d.big_min = det->pp.min_component_size;
         apply_limits(det->limits, &d);
     }
     const FrameDesc* d_table;

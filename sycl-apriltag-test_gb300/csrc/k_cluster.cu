@@ -120,60 +120,35 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     // labels of the tile (16-byte loads of four) and its halo columns, then
     // the size of each label's component: all label loads of a thread are
     // issued before its size gathers
-    // Components that the tile CCL already found to be big within one tile
-    // (F.bigmap) need no size gather: a 4-label item takes its two bitmap
-    // words (255 and 0 forests) with its label load, and only labels whose
-    // block bit is clear (and label 0) read their component's size.
     {
         constexpr int THREADS = BP_W / 4 * BP_H, NQ = BP_SH * (BP_W / 4), NH = BP_SH * 2;
         constexpr int NI = (NQ + NH + THREADS - 1) / THREADS;
-        const uint32_t wpr = ((uint32_t)w / 2 + 31) / 32;
         uint4 lv[NI];
-        uint32_t bm[NI];  // the item's block bits: 255 forest in bits 0-1, 0 forest in bits 2-3
 #pragma unroll
         for (int k = 0; k < NI; k++) {
             const int it = threadIdx.x + k * THREADS;
             lv[k] = make_uint4(0u, 0u, 0u, 0u);
-            uint2 words = make_uint2(0u, 0u);
-            int x = 0;
             if (it < NQ) {
-                const int r = it / (BP_W / 4), y = y0 + r;
-                x = x0 + 4 * (it % (BP_W / 4));
-                if (y < h && x < w) {
-                    lv[k] = __ldg(reinterpret_cast<const uint4*>(F.labels + (size_t)y * w + x));
-                    if (F.bigmap)
-                        words = __ldg(reinterpret_cast<const uint2*>(F.bigmap + 2 * ((size_t)(y >> 1) * wpr + (uint32_t)x / 64)));
-                }
+                const int r = it / (BP_W / 4), y = y0 + r, x = x0 + 4 * (it % (BP_W / 4));
+                if (y < h && x < w) lv[k] = __ldg(reinterpret_cast<const uint4*>(F.labels + (size_t)y * w + x));
             } else if (it < NQ + NH) {
-                const int hi = it - NQ, y = y0 + (hi >> 1);
-                x = (hi & 1) ? x0 + BP_W : x0 - 1;
-                if (y < h && x >= 0 && x < w) {
-                    lv[k].x = __ldg(F.labels + (size_t)y * w + x);
-                    if (F.bigmap)
-                        words = __ldg(reinterpret_cast<const uint2*>(F.bigmap + 2 * ((size_t)(y >> 1) * wpr + (uint32_t)x / 64)));
-                }
+                const int hi = it - NQ, y = y0 + (hi >> 1), x = (hi & 1) ? x0 + BP_W : x0 - 1;
+                if (y < h && x >= 0 && x < w) lv[k].x = __ldg(F.labels + (size_t)y * w + x);
             }
-            // the (up to) two blocks of the item: x / 2 and x / 2 + 1
-            const uint32_t b = ((uint32_t)x >> 1) & 31u;
-            bm[k] = ((words.x >> b) & 3u) | (((words.y >> b) & 3u) << 2);
         }
 #pragma unroll
         for (int k = 0; k < NI; k++) {
             const int it = threadIdx.x + k * THREADS;
-            // j: 0 for the item's first block, 1 for its second
-            auto tag = [&](uint32_t v, int j) {
-                if (v != 0u && ((bm[k] >> ((v >> 31) ? j : 2 + j)) & 1u)) return v | BP_BIG;
-                return v | (__ldg(F.sizes + (v & LABEL_VALUE_MASK)) >= min_size ? BP_BIG : 0u);
-            };
+            auto tag = [&](uint32_t v) { return v | (__ldg(F.sizes + (v & LABEL_VALUE_MASK)) >= min_size ? BP_BIG : 0u); };
             if (it < NQ) {
                 const int r = it / (BP_W / 4), c = 1 + 4 * (it % (BP_W / 4));
-                lab[r][c] = tag(lv[k].x, 0);
-                lab[r][c + 1] = tag(lv[k].y, 0);
-                lab[r][c + 2] = tag(lv[k].z, 1);
-                lab[r][c + 3] = tag(lv[k].w, 1);
+                lab[r][c] = tag(lv[k].x);
+                lab[r][c + 1] = tag(lv[k].y);
+                lab[r][c + 2] = tag(lv[k].z);
+                lab[r][c + 3] = tag(lv[k].w);
             } else if (it < NQ + NH) {
                 const int hi = it - NQ;
-                lab[hi >> 1][(hi & 1) ? BP_W + 1 : 0] = tag(lv[k].x, 0);
+                lab[hi >> 1][(hi & 1) ? BP_W + 1 : 0] = tag(lv[k].x);
             }
         }
     }

@@ -375,15 +375,6 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         if (last_b && cb) atomicAdd(&cnt[rb], cb);
     }
     __syncthreads();
-    if (F.bigmap) {
-        // blocks whose component already has big_min pixels in this tile
-        const unsigned mw = __ballot_sync(0xFFFFFFFFu, live && (L.info & 0xFu) && cnt[rw] >= F.big_min);
-        const unsigned mb = __ballot_sync(0xFFFFFFFFu, live && (L.info & 0xF00u) && cnt[rb] >= F.big_min);
-        if (lane == 0 && by < h / 2) {
-            const uint32_t wpr = ((uint32_t)w / 2 + 31) / 32;
-            *reinterpret_cast<uint2*>(F.bigmap + 2 * ((size_t)by * wpr + (uint32_t)bx0 / 32)) = make_uint2(mw, mb);
-        }
-    }
     if (live) {
         auto gslot = [&](uint32_t s) {
             uint32_t lb = s >> 1;
