@@ -443,8 +443,17 @@ def main():
                                "own_gbs": sbytes.get(k, 0) / (stage_ms[k] / 1000.0) / 1e9}
                            for k in vbytes if stage_ms.get(k, 0) > 0}}
 
-    # --- plain single-frame path: latency per frame, L2 flushed in between
-    plain = plain_path(args, Detector(w, h, config=cfg), frames, stream) if args.plain_frames > 0 else None
+    # --- plain single-frame path: latency per frame, L2 flushed in between,
+    # with launch shapes tuned for one frame (its own best, not the batch's)
+    plain = None
+    if args.plain_frames > 0:
+        det1 = Detector(w, h, config=cfg)
+        plain_tuning = None
+        if not args.no_tune:
+            from atag import autotune
+            plain_tuning = autotune.autotune(det1, frames[:1], reps=20, passes=2)["tuning"]
+        plain = plain_path(args, det1, frames, stream)
+        plain["tuning"] = plain_tuning
 
     # --- e2e: public API, host buffers in and out.  Two detectors take
     # alternate steps: a step's frames are copied in (pinned H2D) on a copy
