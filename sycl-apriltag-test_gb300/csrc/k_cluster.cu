@@ -96,6 +96,7 @@ template <int BP_H>
 __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32_t min_size) {
     constexpr int BP_SH = BP_H + 1;
     constexpr int BP_STAGE = BP_W * BP_H * 4;  // at most 4 points per pixel
+    constexpr int BP_WSTAGE = 2 * BP_W * 4;    // the part of one warp (two tile rows)
     // frame from blockIdx.x, tile from blockIdx.y: CTAs are dispatched
     // frame-fastest, so the tiles in flight at once span every frame of the
     // batch and a frame's later tiles start after its first ones published
@@ -112,8 +113,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     __shared__ uint32_t lab[BP_SH][BP_SW];
     __shared__ PairTableSmem T;
     __shared__ uint32_t stage[BP_STAGE];
-    __shared__ uint32_t red[33];
-    __shared__ uint32_t s_base;
+    __shared__ uint32_t s_nall;
     __shared__ unsigned long long s_dead[DEAD_PAIRS];
     const bool track_dead = !F.stage_outputs && F.dead_pairs;
 
@@ -155,6 +155,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     // pairs that earlier tiles already pushed over the cluster size limit
     // (a snapshot: a pair published later is simply processed in full)
     if (threadIdx.x < DEAD_PAIRS) s_dead[threadIdx.x] = track_dead ? __ldcg(F.dead_pairs + threadIdx.x) : EMPTY_KEY;
+    if (threadIdx.x == 0) s_nall = 0;
     for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
         T.key[i] = EMPTY_KEY;
         T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
@@ -219,27 +220,36 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     const uint32_t dp = dr >> 1;
     const uint32_t d0 = dp & (dr >> 2), d1 = dp & db, d2 = dp & (db >> 1), d3 = dp & (db >> 2);
     const uint32_t staged = masks & ~(spread(d0) | (spread(d1) << 1) | (spread(d2) << 2) | (spread(d3) << 3));
-    // one scan of both counts (a CTA has at most 4096 points: no carry)
-    uint32_t both;
-    const uint32_t pos0 =
-        block_exclusive_scan_u32((uint32_t)__popc(staged) | ((uint32_t)__popc(masks) << 16), red, &both) & 0xFFFFu;
-    const uint32_t nst = both & 0xFFFFu, nall = both >> 16;
+    // Each warp owns two tile rows: it lists its staged points in its own
+    // part of the staging array (warp scan) and aggregates them itself, so
+    // no CTA barrier separates the masks from the rounds.
+    const int warp = threadIdx.x >> 5;
+    uint32_t* wst = stage + warp * BP_WSTAGE;
+    const uint32_t ns = (uint32_t)__popc(staged);
+    uint32_t incl = ns;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t nst = __shfl_sync(0xFFFFFFFFu, incl, 31);
     {
-        uint32_t pos = pos0;
+        uint32_t pos = incl - ns;
         for (uint32_t mm = staged; mm; mm &= mm - 1) {
             const int bit = __ffs(mm) - 1;
-            stage[pos++] = stage_entry(0, cbase + (bit >> 2), r, bit & 3, 0);
+            wst[pos++] = stage_entry(0, cbase + (bit >> 2), r, bit & 3, 0);
         }
+        const uint32_t nall_w = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)__popc(masks));
+        if (lane == 0 && nall_w) atomicAdd(&s_nall, nall_w);
     }
-    __syncthreads();
-    // Then the CTA's warps take the staged points 32 at a time (round k of a
-    // warp covers points 32 (k W + warp) ..): pair key, CTA table slot (one
-    // insert per distinct key of the round) and the per-pair sums of the
-    // round's points, merged into the table by one lane per key.
-    for (uint32_t b0 = threadIdx.x & ~31u; b0 < nst; b0 += blockDim.x) {
+    __syncwarp();
+    // The warp takes its staged points 32 at a time: pair key, CTA table
+    // slot (one insert per distinct key of the round) and the per-pair sums
+    // of the round's points, merged into the table by one lane per key.
+    for (uint32_t b0 = 0; b0 < nst; b0 += 32) {
         const uint32_t i = b0 + (uint32_t)lane;
         const bool v = i < nst;
-        uint32_t e = v ? stage[i] : 0u;
+        uint32_t e = v ? wst[i] : 0u;
         const int xo = (int)(e & 63), ro = (int)((e >> 6) & 15), t = (int)((e >> 10) & 3), c = xo + 1;
         const int rr = ro + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
         const uint32_t p = lab[ro][c], q = lab[rr][cc];
@@ -251,7 +261,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         static_assert(DEAD_PAIRS == 2, "the test below reads both entries");
         const bool dead = v && (key == s_dead[0] || key == s_dead[1]);
         if (__all_sync(0xFFFFFFFFu, dead || !v)) {
-            if (v) stage[i] = e | STAGE_DIRECT;
+            if (v) wst[i] = e | STAGE_DIRECT;
             continue;
         }
         const unsigned m = __match_any_sync(0xFFFFFFFFu, key);
@@ -276,7 +286,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         } else {
             e |= (uint32_t)ls << 13;
         }
-        if (v) stage[i] = e;
+        if (v) wst[i] = e;
         const bool a = v && ls >= 0;
         const uint32_t cnt = __reduce_add_sync(m, a ? 1u : 0u);
         const uint32_t xmn = __reduce_min_sync(m, xd), xmx = __reduce_max_sync(m, xd);
@@ -300,6 +310,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     // (cluster_bounds.h:92-93,102) can never survive; its points are counted
     // but not listed.
     const uint32_t max_pixels = 2u * (2u * (uint32_t)w + 2u * (uint32_t)h);
+    if (threadIdx.x == 0 && s_nall) atomicAdd(F.counters + CNT_ALLPOINTS, s_nall);
     for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
         unsigned long long key = T.key[i];
         if (key == EMPTY_KEY) continue;
@@ -320,31 +331,33 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     }
     __syncthreads();
 
-    // D: list the points of live pairs (contiguous chunk per thread)
-    const uint32_t per = (nst + blockDim.x - 1) / blockDim.x;
-    const uint32_t i0 = min(nst, threadIdx.x * per), i1 = min(nst, i0 + per);
+    // D: each warp lists the points of live pairs from its own staging
+    // part: a count pass, one atomic for the warp's place in the list, then
+    // the writes in the same order
+    auto live_at = [&](uint32_t i) {
+        if (i >= nst) return false;
+        const uint32_t e = wst[i];
+        return !(e & STAGE_DIRECT) && T.gslot[(e >> 13) & 255] != INVALID;
+    };
     uint32_t nlive = 0;
-    for (uint32_t i = i0; i < i1; i++) {
-        const uint32_t e = stage[i];
-        nlive += !(e & STAGE_DIRECT) && T.gslot[(e >> 13) & 255] != INVALID;
+    for (uint32_t b0 = 0; b0 < nst; b0 += 32) nlive += (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, live_at(b0 + lane)));
+    if (nlive == 0) return;
+    uint32_t at = 0;
+    if (lane == 0) {
+        at = atomicAdd(F.counters + CNT_POINTS, nlive);
+        if ((unsigned long long)at + nlive > F.point_cap) atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
     }
-    uint32_t total;
-    const uint32_t off = block_exclusive_scan_u32(nlive, red, &total);
-    if (threadIdx.x == 0) {
-        uint32_t b = total ? atomicAdd(F.counters + CNT_POINTS, total) : 0u;
-        if (nall) atomicAdd(F.counters + CNT_ALLPOINTS, nall);
-        if ((unsigned long long)b + total > F.point_cap) atomicOr(status, ATAG_DEVFLAG_POINT_OVERFLOW);
-        s_base = b;
-    }
-    __syncthreads();
-    uint32_t at = s_base + off;
-    for (uint32_t i = i0; i < i1; i++) {
-        const uint32_t e = stage[i];
-        if (e & STAGE_DIRECT) continue;
-        const uint32_t gs = T.gslot[(e >> 13) & 255];
-        if (gs == INVALID) continue;
-        if (at < F.point_cap) F.points[at] = ((unsigned long long)gs << 32) | stage_packed(e, x0, y0);
-        at++;
+    at = __shfl_sync(0xFFFFFFFFu, at, 0);
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint32_t b0 = 0; b0 < nst; b0 += 32) {
+        const uint32_t i = b0 + (uint32_t)lane;
+        const bool lv = live_at(i);
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, lv);
+        if (lv) {
+            const uint32_t e = wst[i], dst = at + (uint32_t)__popc(m & lt);
+            if (dst < F.point_cap) F.points[dst] = ((unsigned long long)T.gslot[(e >> 13) & 255] << 32) | stage_packed(e, x0, y0);
+        }
+        at += (uint32_t)__popc(m);
     }
 }
 

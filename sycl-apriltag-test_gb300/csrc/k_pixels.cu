@@ -240,6 +240,7 @@ __device__ __forceinline__ uint32_t ccl_tiles_y(uint32_t h) { return (h / 2 + CC
 template <int CCL_BY>
 __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     constexpr int CCL_THREADS = CCL_BX * CCL_BY;
+    constexpr unsigned FULL = 0xFFFFFFFFu;
     const FrameDesc& F = fs.get(blockIdx.y);
     const int w = F.width, h = F.height;
     const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y<CCL_BY>(h);
@@ -248,6 +249,7 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     const int x0 = bx0 * 2, y0 = by0 * 2;
 
     constexpr int PH = 2 * CCL_BY + 1, WPR = (2 * CCL_BX + 8) / 4;
+    static_assert(WPR <= 32 && PH <= 3 * CCL_BY, "one word per lane, three rows per warp");
     // rows y0 - 1 .., words of pixels x0 - 4 .. x0 + 2 CCL_BX + 3 (x0 and w
     // are multiples of 4): pixel x of a row is byte x - x0 + 4
     __shared__ uint32_t pixw[PH][WPR];
@@ -256,27 +258,27 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __shared__ uint32_t row_runs[CCL_BY][2];  // S-link ballots of each tile row (255, 0 forest)
     __shared__ uint32_t ulist[CCL_BY][192];   // per row: unions with the row above (slot << 16 | slot)
 
-    // the tile's pixels plus a one-pixel halo (x0 - 1 .. x0 + 2 CCL_BX, y0 - 1
-    // ..), loaded as aligned 32-bit words; all loads of a thread are issued
-    // before any is stored
+    const int tx = threadIdx.x % CCL_BX, ty = threadIdx.x / CCL_BX;  // lane, warp
+    // the tile's pixels plus a one-pixel halo as aligned 32-bit words: warp
+    // ty loads rows ty, ty + CCL_BY (and warp 0 row 2 CCL_BY), one word per
+    // lane; both loads are issued before either is stored
     {
-        constexpr int NI = (PH * WPR + CCL_THREADS - 1) / CCL_THREADS;
         const uint32_t* thr32 = reinterpret_cast<const uint32_t*>(F.thr);
-        uint32_t v[NI];
+        const int xw = x0 - 4 + 4 * tx;
+        const bool colok = tx < WPR && xw >= 0 && xw < w;
+        uint32_t v[3];
 #pragma unroll
-        for (int k = 0; k < NI; k++) {
-            const int i = threadIdx.x + k * CCL_THREADS, r = i / WPR, q = i % WPR;
-            const int y = y0 - 1 + r, xw = x0 - 4 + 4 * q;
-            v[k] = (i < PH * WPR && y >= 0 && y < h && xw >= 0 && xw < w) ? __ldg(thr32 + ((size_t)y * w + xw) / 4)
-                                                                          : 0x7F7F7F7Fu;
+        for (int k = 0; k < 3; k++) {
+            const int row = ty + k * CCL_BY, y = y0 - 1 + row;
+            v[k] = (colok && row < PH && y >= 0 && y < h) ? __ldg(thr32 + (size_t)y * (uint32_t)(w >> 2) + (xw >> 2))
+                                                          : 0x7F7F7F7Fu;
         }
 #pragma unroll
-        for (int k = 0; k < NI; k++) {
-            const int i = threadIdx.x + k * CCL_THREADS;
-            if (i < PH * WPR) pixw[i / WPR][i % WPR] = v[k];
+        for (int k = 0; k < 3; k++) {
+            const int row = ty + k * CCL_BY;
+            if (tx < WPR && row < PH) pixw[row][tx] = v[k];
         }
     }
-    const int tx = threadIdx.x % CCL_BX, ty = threadIdx.x / CCL_BX;
     const int bx = bx0 + tx, by = by0 + ty;
     const bool live = bx < w / 2 && by < h / 2;
     const uint32_t l = threadIdx.x;
@@ -284,20 +286,44 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     cnt[2 * l + 1] = 0;
     __syncthreads();
 
-    BlockLinks L{0, 0, 0};
-    if (live) {
-        const int r0 = 2 * ty + 1, c0 = 2 * tx + 1;
-        L = block_links([&](int dy, int dx) { return (uint32_t)reinterpret_cast<const uint8_t*>(pixw[r0 + dy])[c0 + dx + 3]; },
-                        bx * 2, by * 2, w, h);
-    }
+    // The block's links, computed on bytes: p(x - 1) .. p(x + 2) of pixel
+    // rows y - 1, y and y + 1 (x = 2 bx, y = 2 by) as one word each, and
+    // per byte "is 255" / "is 0" masks.  The neighbour test pixels and
+    // block_links' check masks become: P (up-left) tests p(x-1, y-1) when
+    // TL is valid, Q (up) p(x, y-1) or p(x+1, y-1) when TL or TR is, R
+    // (up-right) p(x+2, y-1) when TR is, S (left) p(x-1, y) or p(x-1, y+1)
+    // when TL or BL is; image edges drop P and S (x = 0), R (x + 2 >= w)
+    // and P, Q, R (y = 0).
+    const int o = 2 * tx + 3, wq = o >> 2, sh = (o & 3) * 8;
+    auto win = [&](int row) { return __funnelshift_r(pixw[row][wq], pixw[row][wq + 1], sh); };
+    const uint32_t vm = win(2 * ty), v0 = win(2 * ty + 1), v1 = win(2 * ty + 2);
+    const uint32_t Wm = __vcmpeq4(vm, FULL), Km = __vcmpeq4(vm, 0u);
+    const uint32_t W0 = __vcmpeq4(v0, FULL), K0 = __vcmpeq4(v0, 0u);
+    const uint32_t W1 = __vcmpeq4(v1, FULL), K1 = __vcmpeq4(v1, 0u);
+    const uint32_t V0 = W0 | K0, V1 = W1 | K1;
+    const bool tl = V0 & 0xFF00u, tr = V0 & 0xFF0000u, bl = V1 & 0xFF00u;
+    const bool gx = bx > 0, gy = by > 0, gr = 2 * bx + 2 < w;
+    const bool cP = live && tl && gx && gy, cQ = live && (tl || tr) && gy, cR = live && tr && gr && gy;
+    const bool cS = live && (tl || bl) && gx;
+    // bit 0 P, 1 Q, 2 R, 3 S
+    auto links = [&](uint32_t M, uint32_t X0, uint32_t X1) {
+        return (cP && (M & 0xFFu) ? 1u : 0u) | (cQ && (M & 0xFFFF00u) ? 2u : 0u) | (cR && (M & 0xFF000000u) ? 4u : 0u) |
+               (cS && ((X0 | X1) & 0xFFu) ? 8u : 0u);
+    };
+    const uint32_t lw = links(Wm, W0, W1), lb = links(Km, K0, K1);
+    // the block's 255 and 0 pixel counts
+    const uint32_t cw = live ? (uint32_t)(__popc(W0 & 0x00FFFF00u) + __popc(W1 & 0x00FFFF00u)) >> 3 : 0u;
+    const uint32_t cb = live ? (uint32_t)(__popc(K0 & 0x00FFFF00u) + __popc(K1 & 0x00FFFF00u)) >> 3 : 0u;
+
     // S links (left neighbour) inside the tile row, which is this warp: a run
     // of blocks that each link to their left neighbour points at its first
     // block, a smaller slot, so the root of a set stays its minimum
     const uint32_t lane = (uint32_t)tx;
-    const unsigned sw = __ballot_sync(0xFFFFFFFFu, live && tx > 0 && (L.wmask & 8u));
-    const unsigned sb = __ballot_sync(0xFFFFFFFFu, live && tx > 0 && (L.bmask & 8u));
-    const unsigned le = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+    const unsigned sw = __ballot_sync(FULL, tx > 0 && (lw & 8u));
+    const unsigned sb = __ballot_sync(FULL, tx > 0 && (lb & 8u));
+    const unsigned le = lane == 31 ? FULL : ((2u << lane) - 1u);
     const uint32_t hw = 31 - __clz(~sw & le), hb = 31 - __clz(~sb & le);  // run heads (lanes)
+    const unsigned mw = le & ~((1u << hw) - 1u), mb = le & ~((1u << hb) - 1u);  // the run up to this lane
     const uint32_t row0 = (uint32_t)ty * CCL_BX;
     const bool last_w = lane == 31 || !((sw >> (lane + 1)) & 1u);  // last block of its run
     const bool last_b = lane == 31 || !((sb >> (lane + 1)) & 1u);
@@ -310,30 +336,17 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __syncthreads();
     // P, Q, R links (up-left, up, up-right) inside the tile.  Every block
     // of a run shares the run's set, so a run needs one union per run of
-    // the row above that any of its blocks links to: the run's last lane
-    // ORs the above-row blocks its lanes link to (segmented scan), keeps the
-    // first linked block of each above run and makes those unions.
+    // the row above that any of its blocks links to: from the row's link
+    // ballots the run's last lane takes the above-row blocks its run links
+    // to, keeps the first linked block of each above run and makes those
+    // unions.
     if (ty > 0) {
-        uint32_t aw = 0, ab = 0;
-        if (live) {
-            const uint32_t me = 1u << lane;
-            if (L.wmask & 2u) aw |= me;
-            if (L.bmask & 2u) ab |= me;
-            if (tx > 0) {
-                if (L.wmask & 1u) aw |= me >> 1;
-                if (L.bmask & 1u) ab |= me >> 1;
-            }
-            if (tx < CCL_BX - 1) {
-                if (L.wmask & 4u) aw |= me << 1;
-                if (L.bmask & 4u) ab |= me << 1;
-            }
-        }
-#pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, aw, o), yb = __shfl_up_sync(0xFFFFFFFFu, ab, o);
-            if (lane >= hw + o) aw |= yw;
-            if (lane >= hb + o) ab |= yb;
-        }
+        const unsigned PW = __ballot_sync(FULL, tx > 0 && (lw & 1u)), QW = __ballot_sync(FULL, lw & 2u);
+        const unsigned RW = __ballot_sync(FULL, tx < CCL_BX - 1 && (lw & 4u));
+        const unsigned PB = __ballot_sync(FULL, tx > 0 && (lb & 1u)), QB = __ballot_sync(FULL, lb & 2u);
+        const unsigned RB = __ballot_sync(FULL, tx < CCL_BX - 1 && (lb & 4u));
+        const uint32_t aw = ((PW & mw) >> 1) | (QW & mw) | ((RW & mw) << 1);
+        const uint32_t ab = ((PB & mb) >> 1) | (QB & mb) | ((RB & mb) << 1);
         const uint32_t up0 = row0 - CCL_BX;
         uint32_t ew = last_w ? (aw & ~((aw << 1) & row_runs[ty - 1][0])) : 0u;
         uint32_t eb = last_b ? (ab & ~((ab << 1) & row_runs[ty - 1][1])) : 0u;
@@ -343,42 +356,42 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         const uint32_t nu = (uint32_t)(__popc(ew) + __popc(eb));
         uint32_t incl = nu;
 #pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-            if (lane >= o) incl += y;
+        for (uint32_t o2 = 1; o2 < 32; o2 <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, o2);
+            if (lane >= o2) incl += y;
         }
         uint32_t at = incl - nu;
         for (; ew; ew &= ew - 1) ulist[ty][at++] = (2 * (row0 + hw)) << 16 | (2 * (up0 + __ffs(ew) - 1));
         for (; eb; eb &= eb - 1) ulist[ty][at++] = (2 * (row0 + hb) + 1) << 16 | (2 * (up0 + __ffs(eb) - 1) + 1);
         __syncwarp();
-        const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
         for (uint32_t k = lane; k < total; k += 32) {
             const uint32_t e = ulist[ty][k];
             uf_union((volatile uint32_t*)par, e >> 16, e & 0xFFFFu, 2u * CCL_THREADS);
         }
     }
     __syncthreads();
+    // roots: a run's head finds it, its other blocks take it from the head
     bool local_capped = false;  // cannot happen: a tile chain visits at most its 2 CCL_THREADS slots
-    uint32_t rw = find_root_volatile((volatile uint32_t*)par, 2 * l, 2u * CCL_THREADS, &local_capped);
-    uint32_t rb = find_root_volatile((volatile uint32_t*)par, 2 * l + 1, 2u * CCL_THREADS, &local_capped);
-    // pixel counts per root: the blocks of a run share its root, so the
-    // run's last lane adds the run's count (segmented warp sum)
+    uint32_t rw = lane == hw ? find_root_volatile((volatile uint32_t*)par, 2 * l, 2u * CCL_THREADS, &local_capped) : 0u;
+    uint32_t rb = lane == hb ? find_root_volatile((volatile uint32_t*)par, 2 * l + 1, 2u * CCL_THREADS, &local_capped) : 0u;
+    rw = __shfl_sync(FULL, rw, hw);
+    rb = __shfl_sync(FULL, rb, hb);
+    // pixel counts per root: the run's last lane adds the run's count, the
+    // sum over the run's lanes of the ballots of each count bit
     {
-        uint32_t cw = __popc(L.info & 0xF), cb = __popc(L.info & 0xF00);
-#pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const uint32_t yw = __shfl_up_sync(0xFFFFFFFFu, cw, o), yb = __shfl_up_sync(0xFFFFFFFFu, cb, o);
-            if (lane >= hw + o) cw += yw;
-            if (lane >= hb + o) cb += yb;
-        }
-        if (last_w && cw) atomicAdd(&cnt[rw], cw);
-        if (last_b && cb) atomicAdd(&cnt[rb], cb);
+        const unsigned w1 = __ballot_sync(FULL, cw & 1u), w2 = __ballot_sync(FULL, cw & 2u), w4 = __ballot_sync(FULL, cw & 4u);
+        const unsigned b1 = __ballot_sync(FULL, cb & 1u), b2 = __ballot_sync(FULL, cb & 2u), b4 = __ballot_sync(FULL, cb & 4u);
+        const uint32_t sw_ = (uint32_t)(__popc(w1 & mw) + 2 * __popc(w2 & mw) + 4 * __popc(w4 & mw));
+        const uint32_t sb_ = (uint32_t)(__popc(b1 & mb) + 2 * __popc(b2 & mb) + 4 * __popc(b4 & mb));
+        if (last_w && sw_) atomicAdd(&cnt[rw], sw_);
+        if (last_b && sb_) atomicAdd(&cnt[rb], sb_);
     }
     __syncthreads();
     if (live) {
         auto gslot = [&](uint32_t s) {
-            uint32_t lb = s >> 1;
-            return (uint32_t)((by0 + lb / CCL_BX) * 2) * (uint32_t)w + (uint32_t)(bx0 + lb % CCL_BX) * 2 + (s & 1);
+            uint32_t lb2 = s >> 1;
+            return (uint32_t)((by0 + lb2 / CCL_BX) * 2) * (uint32_t)w + (uint32_t)(bx0 + lb2 % CCL_BX) * 2 + (s & 1);
         };
         size_t id = (size_t)(by * 2) * w + bx * 2;
         uint2 parents = make_uint2(gslot(rw), gslot(rb));
@@ -387,8 +400,12 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         *reinterpret_cast<uint2*>(F.sizes + id) = sz;
         if (F.stage_outputs) {
             *reinterpret_cast<uint2*>(F.sizes + id + w) = make_uint2(0u, 0u);
-            // the reference keeps the block's information word at scratch[id + w]
-            *reinterpret_cast<uint2*>(F.scratch + id + w) = make_uint2(L.info, 0u);
+            // the reference keeps the block's information word at scratch[id + w]:
+            // bits 0-3 the pixels (TL, TR, BL, BR) that are 255, bits 8-11 those that are 0
+            auto bits = [](uint32_t X0, uint32_t X1) {
+                return ((X0 >> 8) & 1u) | ((X0 >> 15) & 2u) | ((X1 >> 6) & 4u) | ((X1 >> 13) & 8u);
+            };
+            *reinterpret_cast<uint2*>(F.scratch + id + w) = make_uint2(bits(W0, W1) | (bits(K0, K1) << 8), 0u);
         }
     }
 }
