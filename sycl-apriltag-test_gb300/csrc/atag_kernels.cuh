@@ -80,7 +80,19 @@ struct FrameDesc {
     // sizes away from roots).  0 (fused batches): only what later stages
     // read, i.e. parents at even rows and sizes at the roots.
     uint32_t stage_outputs;
+    // Tile CCL edge records (ccl_edge_words(tile rows) words per CCL tile,
+    // see k_pixels.cu): the tile roots and cross-tile links of each tile's
+    // edge blocks, written by the tile pass and read by the border pass.
+    // Null: the border pass reads the thresholded image and the forest.
+    uint32_t* edges;
 };
+
+// Words of one CCL tile's edge record (tiles of 32 blocks x `rows` block
+// rows): per edge block a (255 slot, 0 slot) pair of tile roots whose bits
+// 24-27 hold that forest's P, Q, R, S links: the top row [0, 32), the
+// bottom row [32, 64), the left column [64, 64 + rows), the right column
+// [64 + rows, 64 + 2 rows).
+__host__ __device__ constexpr uint32_t ccl_edge_words(uint32_t rows) { return 2 * (64 + 2 * rows); }
 
 // The frames a launch works on: a device table (batches) or one descriptor
 // passed by value (stage entry points, which must not allocate).  Kernels
@@ -159,6 +171,9 @@ __global__ void k_ccl_border_r8(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_local_r32(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_border_r16(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_border_r32(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_border_edges_r8(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_border_edges_r16(const __grid_constant__ FrameSet fs);
+__global__ void k_ccl_border_edges_r32(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_final(const __grid_constant__ FrameSet fs);
 __global__ void k_boundaries_dense(const __grid_constant__ FrameSet fs, uint32_t min_size);
 

@@ -194,6 +194,11 @@ size_t layout_frame(char* base, uint32_t w, uint32_t h, uint32_t factor, bool ow
     f.cluster_runs = (uint32_t*)take(4ull * c.cluster_cap);
     f.counters = (uint32_t*)take(4ull * CNT_COUNT);
     f.dead_pairs = (unsigned long long*)take(8ull * DEAD_PAIRS);
+    // CCL edge records, sized for the largest of the tile-row choices
+    size_t edge_words = 0;
+    for (uint32_t rows : {8u, 16u, 32u})
+        edge_words = std::max(edge_words, cdiv(w / 2, 32) * cdiv(h / 2, (size_t)rows) * ccl_edge_words(rows));
+    f.edges = (uint32_t*)take(4 * edge_words);
     if (d) *d = f;
     return off;
 }
@@ -920,9 +925,9 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
     STAGE(4);
     {
         const size_t border = tiles_ccl * (32 + 2 * (ccl_rows - 1));
-        if (ccl_rows == 8) k_ccl_border_r8<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
-        else if (ccl_rows == 32) k_ccl_border_r32<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
-        else k_ccl_border_r16<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
+        if (ccl_rows == 8) k_ccl_border_edges_r8<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
+        else if (ccl_rows == 32) k_ccl_border_edges_r32<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
+        else k_ccl_border_edges_r16<<<grid2(cdiv(border, 256), n), 256, 0, s>>>(fs);
         LAUNCHED();
     }
     STAGE(5);

@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256) k_reset_frames(const __grid_constant__ Fr
 constexpr int BP_W = 64;                       // tile width; BP_H (8 or 16) rows is a tuning choice
 constexpr int BP_SW = BP_W + 2;
 constexpr int BP_LC = 64;                      // CTA hash-table entries (a tile has a few dozen pairs; more go straight to the frame's table)
-constexpr uint32_t BP_BIG = 0x40000000u, BP_VALUE = 0x3FFFFFFFu;
+constexpr uint32_t BP_VALUE = 0x3FFFFFFFu;  // label value without the colour bit
 
 struct PairTableSmem {
     unsigned long long key[BP_LC];
@@ -95,8 +95,11 @@ __device__ __forceinline__ uint32_t stage_packed(uint32_t e, uint32_t x0, uint32
 template <int BP_H>
 __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32_t min_size) {
     constexpr int BP_SH = BP_H + 1;
+    constexpr int NW = BP_H / 2;               // warps: two tile rows each
     constexpr int BP_STAGE = BP_W * BP_H * 4;  // at most 4 points per pixel
     constexpr int BP_WSTAGE = 2 * BP_W * 4;    // the part of one warp (two tile rows)
+    constexpr unsigned FULL = 0xFFFFFFFFu;
+    static_assert(BP_W == 64, "two 32-pixel words per row");
     // frame from blockIdx.x, tile from blockIdx.y: CTAs are dispatched
     // frame-fastest, so the tiles in flight at once span every frame of the
     // batch and a frame's later tiles start after its first ones published
@@ -107,83 +110,37 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     if ((int)blockIdx.y >= ntx * nty) return;
     const int x0 = (blockIdx.y % ntx) * BP_W, y0 = (blockIdx.y / ntx) * BP_H;
     uint32_t* status = F.counters + CNT_STATUS;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-    // labels of the tile and its halo; bit 30 (free: label values are
-    // below 2^24) marks a component of at least min_size pixels
+    // labels of the tile and its halo (column 0 = x0 - 1, BP_W + 1 = x0 +
+    // BP_W; row BP_H is the row below the tile), and three bit planes of
+    // them: per row four words, [0] bit 31 = x0 - 1, [1] and [2] = x0 ..
+    // x0 + 63, [3] bit 0 = x0 + 64.  Plane 0: the colour bit (255 pixel),
+    // 1: the component has at least min_size pixels, 2: the label is one of
+    // the two labels of the frame's first pair known to be over the cluster
+    // size limit.
     __shared__ uint32_t lab[BP_SH][BP_SW];
+    __shared__ __align__(16) uint32_t planes[3][BP_SH][4];
     __shared__ PairTableSmem T;
     __shared__ uint32_t stage[BP_STAGE];
     __shared__ uint32_t s_nall;
-    __shared__ unsigned long long s_dead[DEAD_PAIRS];
     const bool track_dead = !F.stage_outputs && F.dead_pairs;
 
-    // labels of the tile (16-byte loads of four) and its halo columns, then
-    // the size of each label's component: all label loads of a thread are
-    // issued before its size gathers
-    {
-        constexpr int THREADS = BP_W / 4 * BP_H, NQ = BP_SH * (BP_W / 4), NH = BP_SH * 2;
-        constexpr int NI = (NQ + NH + THREADS - 1) / THREADS;
-        uint4 lv[NI];
-#pragma unroll
-        for (int k = 0; k < NI; k++) {
-            const int it = threadIdx.x + k * THREADS;
-            lv[k] = make_uint4(0u, 0u, 0u, 0u);
-            if (it < NQ) {
-                const int r = it / (BP_W / 4), y = y0 + r, x = x0 + 4 * (it % (BP_W / 4));
-                if (y < h && x < w) lv[k] = __ldg(reinterpret_cast<const uint4*>(F.labels + (size_t)y * w + x));
-            } else if (it < NQ + NH) {
-                const int hi = it - NQ, y = y0 + (hi >> 1), x = (hi & 1) ? x0 + BP_W : x0 - 1;
-                if (y < h && x >= 0 && x < w) lv[k].x = __ldg(F.labels + (size_t)y * w + x);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < NI; k++) {
-            const int it = threadIdx.x + k * THREADS;
-            auto tag = [&](uint32_t v) { return v | (__ldg(F.sizes + (v & LABEL_VALUE_MASK)) >= min_size ? BP_BIG : 0u); };
-            if (it < NQ) {
-                const int r = it / (BP_W / 4), c = 1 + 4 * (it % (BP_W / 4));
-                lab[r][c] = tag(lv[k].x);
-                lab[r][c + 1] = tag(lv[k].y);
-                lab[r][c + 2] = tag(lv[k].z);
-                lab[r][c + 3] = tag(lv[k].w);
-            } else if (it < NQ + NH) {
-                const int hi = it - NQ;
-                lab[hi >> 1][(hi & 1) ? BP_W + 1 : 0] = tag(lv[k].x);
-            }
-        }
-    }
     // pairs that earlier tiles already pushed over the cluster size limit
-    // (a snapshot: a pair published later is simply processed in full)
-    if (threadIdx.x < DEAD_PAIRS) s_dead[threadIdx.x] = track_dead ? __ldcg(F.dead_pairs + threadIdx.x) : EMPTY_KEY;
-    if (threadIdx.x == 0) s_nall = 0;
-    for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
-        T.key[i] = EMPTY_KEY;
-        T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
-        T.gx[i] = 0; T.gy[i] = 0; T.pxgx[i] = 0; T.gslot[i] = INVALID;
+    // (a snapshot per warp: a pair published later is simply processed in
+    // full; points of a published pair can never survive, so warps that
+    // see different snapshots still agree on the result)
+    unsigned long long dk0 = EMPTY_KEY, dk1 = EMPTY_KEY;
+    if (track_dead) {
+        dk0 = __ldcg(F.dead_pairs);
+        dk1 = __ldcg(F.dead_pairs + 1);
     }
-    __syncthreads();
-
-    // A: enumerate points in the reference's test order (R, BL unless it
-    // would duplicate, B, BR: find_boundaries.cpp:128-150): a 4-bit
-    // emission mask per pixel, positions from one block scan, and each
-    // point (pixel and test) into the staging list.
-    const int lane = threadIdx.x & 31;
-    const int r = threadIdx.x / (BP_W / 4), cbase = (threadIdx.x % (BP_W / 4)) * 4;
-    const int y = y0 + r;
-    // Bit j of cr/br (row r) and cb/bb (row r + 1) is the colour / size
-    // flag of the label at tile column cbase + j, i.e. pixel x0 + cbase - 1
-    // + j; the thread's pixel k is j = k + 1.  A pixel emits test t when it
-    // is in the image and big and the tested neighbour is big and of the
-    // other colour (BL also not when it duplicates the left pixel's BR):
-    // all four pixels' tests are computed at once on these bit rows.
-    // dr/db: the label is one of the two labels of the frame's first pair
-    // known to be over the cluster size limit.  A pair joins a white label
-    // (colour bit | an even root slot) and a black one (an odd root slot, or
-    // label 0 of pixels that are neither 0 nor 255); a boundary point whose
-    // two labels are both in the set is a point of that pair.
-    uint32_t dW = 0xFFFFFFFFu, dK = 0xFFFFFFFFu;
+    // a pair joins a white label (colour bit | an even root slot) and a
+    // black one (an odd root slot, or label 0 of pixels that are neither 0
+    // nor 255)
+    uint32_t dW = FULL, dK = FULL;
     {
-        const uint32_t kA = (uint32_t)(s_dead[0] >> 32), kB = (uint32_t)s_dead[0];
+        const uint32_t kA = (uint32_t)(dk0 >> 32), kB = (uint32_t)dk0;
         if ((kA ^ kB) & 1u) {
             dW = LABEL_PIXEL_MASK | ((kA & 1u) ? kB : kA);
             dK = (kA & 1u) ? kA : kB;
@@ -192,54 +149,116 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
             dK = 0u;
         }
     }
-    uint32_t cr = 0, br = 0, cb = 0, bb = 0, dr = 0, db = 0;
-#pragma unroll
-    for (int j = 0; j < 6; j++) {
-        const uint32_t a = lab[r][cbase + j], b = lab[r + 1][cbase + j];
-        cr |= (a >> 31) << j;
-        br |= ((a >> 30) & 1u) << j;
-        cb |= (b >> 31) << j;
-        bb |= ((b >> 30) & 1u) << j;
-        const uint32_t al = a & ~BP_BIG, bl = b & ~BP_BIG;
-        dr |= (uint32_t)(al == dW || al == dK) << j;
-        db |= (uint32_t)(bl == dW || bl == dK) << j;
+    if (threadIdx.x == 0) s_nall = 0;
+    for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
+        T.key[i] = EMPTY_KEY;
+        T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
+        T.gx[i] = 0; T.gy[i] = 0; T.pxgx[i] = 0; T.gslot[i] = INVALID;
     }
-    uint32_t live = (y < h && x0 + cbase < w) ? 0xFu : 0u;  // w and x0 + cbase are multiples of 4
-    if (x0 + cbase == 0) live &= ~1u;                          // column 0 is never processed
-    live &= br >> 1;
-    const uint32_t cp = cr >> 1;
-    const uint32_t dup = (cr ^ (cb >> 1)) & br & (bb >> 1);
-    const uint32_t m0 = ((cr >> 2) ^ cp) & (br >> 2) & live;             // R
-    const uint32_t m1 = (cb ^ cp) & bb & ~dup & live;                    // BL
-    const uint32_t m2 = ((cb >> 1) ^ cp) & (bb >> 1) & live;             // B
-    const uint32_t m3 = ((cb >> 2) ^ cp) & (bb >> 2) & live;             // BR
-    // bit 4 k + t of masks: test t of pixel k
-    auto spread = [](uint32_t v) { return (v & 1u) | ((v & 2u) << 3) | ((v & 4u) << 6) | ((v & 8u) << 9); };
-    const uint32_t masks = spread(m0) | (spread(m1) << 1) | (spread(m2) << 2) | (spread(m3) << 3);
-    // points of that pair are counted but not staged
-    const uint32_t dp = dr >> 1;
-    const uint32_t d0 = dp & (dr >> 2), d1 = dp & db, d2 = dp & (db >> 1), d3 = dp & (db >> 2);
-    const uint32_t staged = masks & ~(spread(d0) | (spread(d1) << 1) | (spread(d2) << 2) | (spread(d3) << 3));
-    // Each warp owns two tile rows: it lists its staged points in its own
-    // part of the staging array (warp scan) and aggregates them itself, so
-    // no CTA barrier separates the masks from the rounds.
-    const int warp = threadIdx.x >> 5;
+    // Loads: unit u < 2 BP_SH is a 32-pixel word of a row (one label per
+    // lane, coalesced), 2 BP_SH and 2 BP_SH + 1 are the left and right halo
+    // columns (lane = row).  Labels out of the image are 0, as the
+    // reference reads them.  All loads of a warp are issued before its size
+    // gathers, and the planes come from ballots.
+    {
+        constexpr int NU = 2 * BP_SH + 2, PER = (NU + NW - 1) / NW;
+        uint32_t v[PER];
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int u = warp + NW * j;
+            int x = -1, y = h;
+            if (u < 2 * BP_SH) {
+                x = x0 + 32 * (u & 1) + lane;
+                y = y0 + (u >> 1);
+            } else if (u < NU && lane < BP_SH) {
+                x = (u & 1) ? x0 + BP_W : x0 - 1;
+                y = y0 + lane;
+            }
+            v[j] = (x >= 0 && x < w && y < h) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const int u = warp + NW * j;
+            if (u >= NU) break;
+            const uint32_t lv = v[j];
+            const unsigned pc = __ballot_sync(FULL, lv & LABEL_PIXEL_MASK);
+            const unsigned pb = __ballot_sync(FULL, __ldg(F.sizes + (lv & LABEL_VALUE_MASK)) >= min_size);
+            const unsigned pd = __ballot_sync(FULL, lv == dW || lv == dK);
+            if (u < 2 * BP_SH) {
+                const int r = u >> 1, q = 1 + (u & 1);
+                lab[r][q == 1 ? 1 + lane : 33 + lane] = lv;
+                if (lane < 3) planes[lane][r][q] = lane == 0 ? pc : (lane == 1 ? pb : pd);
+            } else if (lane < BP_SH) {
+                const bool right = u & 1;
+                lab[lane][right ? BP_W + 1 : 0] = lv;
+                const int q = right ? 3 : 0, sh = right ? 0 : 31;
+                planes[0][lane][q] = ((pc >> lane) & 1u) << sh;
+                planes[1][lane][q] = ((pb >> lane) & 1u) << sh;
+                planes[2][lane][q] = ((pd >> lane) & 1u) << sh;
+            }
+        }
+    }
+    __syncthreads();
+
+    // A: enumerate points in the reference's test order (R, BL unless it
+    // would duplicate, B, BR: find_boundaries.cpp:128-150).  Lane (rl, k,
+    // t, half) of warp w takes 16 pixels of the 32-pixel word k of tile row
+    // 2 w + rl and test t: a pixel emits test t when it is in the image and
+    // big and the tested neighbour is big and of the other colour (BL also
+    // not when it duplicates the left pixel's BR), computed for the word at
+    // once on the bit planes.  Points of the frame's first over-limit pair
+    // are counted but not staged.
+    const int rl = lane >> 4, k = (lane >> 3) & 1, t = (lane >> 1) & 3, half = lane & 1;
+    const int r = 2 * warp + rl;
+    uint32_t mt, st;
+    {
+        const int xb = x0 + 32 * k;
+        // word k of a plane row and its neighbour-shifted forms
+        auto word = [&](int p, int row, uint32_t& L, uint32_t& C, uint32_t& R) {
+            const uint4 q4 = *reinterpret_cast<const uint4*>(planes[p][row]);
+            const uint32_t prev = k ? q4.y : q4.x, next = k ? q4.w : q4.z;
+            C = k ? q4.z : q4.y;
+            L = __funnelshift_l(prev, C, 1);  // bit i: pixel xb + i - 1
+            R = __funnelshift_r(C, next, 1);  // bit i: pixel xb + i + 1
+        };
+        uint32_t c0L, c0, c0R, b0L, b0, b0R, d0L, d0, d0R;
+        word(0, r, c0L, c0, c0R);
+        word(1, r, b0L, b0, b0R);
+        word(2, r, d0L, d0, d0R);
+        uint32_t live = (y0 + r < h) ? (xb + 32 <= w ? FULL : (xb < w ? ((1u << (w - xb)) - 1u) : 0u)) : 0u;
+        if (xb == 0) live &= ~1u;  // column 0 is never processed
+        live &= b0 & (half ? 0xFFFF0000u : 0x0000FFFFu);
+        // the tested neighbour of test t: R (x + 1, y), BL (x - 1, y + 1),
+        // B (x, y + 1), BR (x + 1, y + 1)
+        uint32_t nc = c0R, nbg = b0R, nd = d0R;
+        uint32_t c1L, c1, c1R, b1L, b1, b1R, d1L, d1, d1R;
+        word(0, r + 1, c1L, c1, c1R);
+        word(1, r + 1, b1L, b1, b1R);
+        word(2, r + 1, d1L, d1, d1R);
+        if (t == 1) { nc = c1L; nbg = b1L; nd = d1L; }
+        if (t == 2) { nc = c1; nbg = b1; nd = d1; }
+        if (t == 3) { nc = c1R; nbg = b1R; nd = d1R; }
+        // BL is not emitted where the left pixel's BR covers the same pair
+        const uint32_t keep = t == 1 ? ~((c0L ^ c1) & b0L & b1) : FULL;
+        mt = (nc ^ c0) & nbg & live & keep;
+        st = mt & ~(d0 & nd);
+    }
+    // Each warp lists its staged points in its own part of the staging
+    // array (warp scan) and aggregates them itself, so no CTA barrier
+    // separates the masks from the rounds.
     uint32_t* wst = stage + warp * BP_WSTAGE;
-    const uint32_t ns = (uint32_t)__popc(staged);
+    const uint32_t ns = (uint32_t)__popc(st);
     uint32_t incl = ns;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+        const uint32_t v = __shfl_up_sync(FULL, incl, o);
         if (lane >= o) incl += v;
     }
-    const uint32_t nst = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const uint32_t nst = __shfl_sync(FULL, incl, 31);
     {
         uint32_t pos = incl - ns;
-        for (uint32_t mm = staged; mm; mm &= mm - 1) {
-            const int bit = __ffs(mm) - 1;
-            wst[pos++] = stage_entry(0, cbase + (bit >> 2), r, bit & 3, 0);
-        }
-        const uint32_t nall_w = __reduce_add_sync(0xFFFFFFFFu, (uint32_t)__popc(masks));
+        for (uint32_t mm = st; mm; mm &= mm - 1) wst[pos++] = stage_entry(0, 32 * k + __ffs(mm) - 1, r, t, 0);
+        const uint32_t nall_w = __reduce_add_sync(FULL, (uint32_t)__popc(mt));
         if (lane == 0 && nall_w) atomicAdd(&s_nall, nall_w);
     }
     __syncwarp();
@@ -259,7 +278,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         // a round whose points all belong to pairs already over the limit
         // contributes nothing: its points are neither aggregated nor listed
         static_assert(DEAD_PAIRS == 2, "the test below reads both entries");
-        const bool dead = v && (key == s_dead[0] || key == s_dead[1]);
+        const bool dead = v && (key == dk0 || key == dk1);
         if (__all_sync(0xFFFFFFFFu, dead || !v)) {
             if (v) wst[i] = e | STAGE_DIRECT;
             continue;

@@ -257,6 +257,7 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __shared__ uint32_t cnt[2 * CCL_THREADS];
     __shared__ uint32_t row_runs[CCL_BY][2];  // S-link ballots of each tile row (255, 0 forest)
     __shared__ uint32_t ulist[CCL_BY][192];   // per row: unions with the row above (slot << 16 | slot)
+    __shared__ uint8_t s_links[CCL_THREADS];  // the blocks' links (edge records)
 
     const int tx = threadIdx.x % CCL_BX, ty = threadIdx.x / CCL_BX;  // lane, warp
     // the tile's pixels plus a one-pixel halo as aligned 32-bit words: warp
@@ -311,6 +312,7 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
                (cS && ((X0 | X1) & 0xFFu) ? 8u : 0u);
     };
     const uint32_t lw = links(Wm, W0, W1), lb = links(Km, K0, K1);
+    s_links[threadIdx.x] = (uint8_t)(lw | (lb << 4));
     // the block's 255 and 0 pixel counts
     const uint32_t cw = live ? (uint32_t)(__popc(W0 & 0x00FFFF00u) + __popc(W1 & 0x00FFFF00u)) >> 3 : 0u;
     const uint32_t cb = live ? (uint32_t)(__popc(K0 & 0x00FFFF00u) + __popc(K1 & 0x00FFFF00u)) >> 3 : 0u;
@@ -388,13 +390,25 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         if (last_b && sb_) atomicAdd(&cnt[rb], sb_);
     }
     __syncthreads();
+    auto gslot = [&](uint32_t s) {
+        uint32_t lb2 = s >> 1;
+        return (uint32_t)((by0 + lb2 / CCL_BX) * 2) * (uint32_t)w + (uint32_t)(bx0 + lb2 % CCL_BX) * 2 + (s & 1);
+    };
+    const uint2 parents = make_uint2(gslot(rw), gslot(rb));
+    if (F.edges) {
+        // the edge record: tile roots of the edge blocks, with the block's
+        // links of that forest in bits 24-27 (slots are below 2^24); links
+        // that leave the tile are the border pass's work
+        uint2* rec = reinterpret_cast<uint2*>(F.edges + (size_t)blockIdx.x * ccl_edge_words(CCL_BY));
+        const uint32_t lk = s_links[threadIdx.x];
+        const uint2 e = make_uint2(parents.x | ((lk & 15u) << 24), parents.y | ((lk >> 4) << 24));
+        if (ty == 0) rec[tx] = e;
+        if (ty == CCL_BY - 1) rec[32 + tx] = e;
+        if (tx == 0) rec[64 + ty] = e;
+        if (tx == CCL_BX - 1) rec[64 + CCL_BY + ty] = e;
+    }
     if (live) {
-        auto gslot = [&](uint32_t s) {
-            uint32_t lb2 = s >> 1;
-            return (uint32_t)((by0 + lb2 / CCL_BX) * 2) * (uint32_t)w + (uint32_t)(bx0 + lb2 % CCL_BX) * 2 + (s & 1);
-        };
         size_t id = (size_t)(by * 2) * w + bx * 2;
-        uint2 parents = make_uint2(gslot(rw), gslot(rb));
         *reinterpret_cast<uint2*>(F.scratch + id) = parents;
         uint2 sz = make_uint2(rw == 2 * l ? cnt[2 * l] : 0u, rb == 2 * l + 1 ? cnt[2 * l + 1] : 0u);
         *reinterpret_cast<uint2*>(F.sizes + id) = sz;
@@ -405,7 +419,9 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
             auto bits = [](uint32_t X0, uint32_t X1) {
                 return ((X0 >> 8) & 1u) | ((X0 >> 15) & 2u) | ((X1 >> 6) & 4u) | ((X1 >> 13) & 8u);
             };
-            *reinterpret_cast<uint2*>(F.scratch + id + w) = make_uint2(bits(W0, W1) | (bits(K0, K1) << 8), 0u);
+            const uint32_t u0 = win(2 * ty + 1), u1 = win(2 * ty + 2);  // rows y, y + 1 again
+            *reinterpret_cast<uint2*>(F.scratch + id + w) =
+                make_uint2(bits(__vcmpeq4(u0, FULL), __vcmpeq4(u1, FULL)) | (bits(__vcmpeq4(u0, 0u), __vcmpeq4(u1, 0u)) << 8), 0u);
         }
     }
 }
@@ -466,6 +482,101 @@ __device__ __forceinline__ void ccl_border_impl(const FrameSet& fs) {
             kb[2 * n] = lw ? par[nid] : 0u;
             ka[2 * n + 1] = rsb;
             kb[2 * n + 1] = lb ? par[nid + 1] : 0u;
+            const unsigned long long kw = lw ? ((unsigned long long)ka[2 * n] << 32 | kb[2 * n]) : ~0ull;
+            const unsigned long long kk = lb ? ((unsigned long long)ka[2 * n + 1] << 32 | kb[2 * n + 1]) : ~0ull;
+            const unsigned long long pw = __shfl_up_sync(0xFFFFFFFFu, kw, 1), pb = __shfl_up_sync(0xFFFFFFFFu, kk, 1);
+            if (lw && (lane == 0 || pw != kw)) need |= 1u << (2 * n);
+            if (lb && (lane == 0 || pb != kk)) need |= 2u << (2 * n);
+        }
+        const uint32_t nu = (uint32_t)__popc(need);
+        uint32_t incl = nu;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t at = incl - nu;
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if (need & (1u << k)) blist[warp][at++] = make_uint2(ka[k], kb[k]);
+        __syncwarp();
+        const uint32_t nlist = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        for (uint32_t k = (uint32_t)lane; k < nlist; k += 32) {
+            const uint2 e = blist[warp][k];
+            ok &= uf_union(par, e.x, e.y, cap);
+        }
+        __syncwarp();
+    }
+    if (!ok && F.counters) atomicOr(F.counters + CNT_STATUS, ATAG_DEVFLAG_UF_ITERATION_CAP);
+}
+
+// The border merge from the tiles' edge records: the same unions as
+// ccl_border_impl, with each edge block's links and tile roots, and its
+// neighbours' tile roots, read from the records (contiguous per tile edge)
+// instead of the image and the forest.  A neighbour across the top edge is
+// on the bottom row of the tile above (above-left / above-right for the
+// corner blocks' P / R), one across the left edge on the left tile's right
+// column, one across the right edge on the right tile's left column.
+template <int CCL_BY>
+__device__ __forceinline__ void ccl_border_edges_impl(const FrameSet& fs) {
+    constexpr int PER = CCL_BX + 2 * (CCL_BY - 1);
+    constexpr uint32_t EW = ccl_edge_words(CCL_BY), SLOT = 0xFFFFFFu;
+    const FrameDesc& F = fs.get(blockIdx.y);
+    const int w = F.width, h = F.height;
+    const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y<CCL_BY>(h);
+    const int total = ntx * nty * PER;
+    volatile uint32_t* par = F.scratch;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ uint2 blist[8][8 * 32];  // per warp: the unions of one pass (8 per lane at most)
+    const uint32_t cap = uf_cap_of(F);
+    bool ok = true;
+    // record entry idx of a tile: [0, 32) top row, [32, 64) bottom row,
+    // [64, 64 + rows) left column, [64 + rows, 64 + 2 rows) right column
+    auto entry = [&](int tile, int idx) { return reinterpret_cast<const uint2*>(F.edges + (size_t)tile * EW)[idx]; };
+    // warp-uniform trip count: lanes past the end take part in the votes
+    for (int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < total; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + lane;
+        uint32_t links = 0;
+        uint2 mine = make_uint2(0u, 0u), nbr[4] = {};
+        if (i < total) {
+            const int tile = i / PER, k = i % PER, up = tile - ntx;
+            uint32_t keep;
+            if (k < CCL_BX) {  // top row: P, Q, R leave the tile; S too in column 0
+                mine = entry(tile, k);
+                keep = k == 0 ? 0xFFu : 0x77u;
+            } else if (k < CCL_BX + CCL_BY - 1) {  // left column: P and S
+                mine = entry(tile, 64 + (k - CCL_BX + 1));
+                keep = 0x99u;
+            } else {  // right column: R
+                mine = entry(tile, 64 + CCL_BY + (k - CCL_BX - CCL_BY + 2));
+                keep = 0x44u;
+            }
+            links = ((mine.x >> 24) | ((mine.y >> 24) << 4)) & keep;
+            if (k < CCL_BX) {
+                const int tx = k;
+                if (links & 0x11u) nbr[0] = tx > 0 ? entry(up, 32 + tx - 1) : entry(up - 1, 32 + CCL_BX - 1);
+                if (links & 0x22u) nbr[1] = entry(up, 32 + tx);
+                if (links & 0x44u) nbr[2] = tx < CCL_BX - 1 ? entry(up, 32 + tx + 1) : entry(up + 1, 32);
+                if (links & 0x88u) nbr[3] = entry(tile - 1, 64 + CCL_BY);
+            } else if (k < CCL_BX + CCL_BY - 1) {
+                const int ty = k - CCL_BX + 1;
+                if (links & 0x11u) nbr[0] = entry(tile - 1, 64 + CCL_BY + ty - 1);
+                if (links & 0x88u) nbr[3] = entry(tile - 1, 64 + CCL_BY + ty);
+            } else {
+                const int ty = k - CCL_BX - CCL_BY + 2;
+                if (links & 0x44u) nbr[2] = entry(tile + 1, 64 + ty - 1);
+            }
+        }
+        // the lane's unions (up to 4 neighbours x 2 forests) into the warp's
+        // list, skipping one the lane before makes too, then one per lane
+        uint32_t ka[8], kb[8], need = 0;
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+            const bool lw = links & (1u << n), lb = links & (16u << n);
+            ka[2 * n] = mine.x & SLOT;
+            kb[2 * n] = lw ? nbr[n].x & SLOT : 0u;
+            ka[2 * n + 1] = mine.y & SLOT;
+            kb[2 * n + 1] = lb ? nbr[n].y & SLOT : 0u;
             const unsigned long long kw = lw ? ((unsigned long long)ka[2 * n] << 32 | kb[2 * n]) : ~0ull;
             const unsigned long long kk = lb ? ((unsigned long long)ka[2 * n + 1] << 32 | kb[2 * n + 1]) : ~0ull;
             const unsigned long long pw = __shfl_up_sync(0xFFFFFFFFu, kw, 1), pb = __shfl_up_sync(0xFFFFFFFFu, kk, 1);
@@ -608,11 +719,14 @@ __global__ void __launch_bounds__(256) k_boundaries_dense(const __grid_constant_
     }
 }
 
-__global__ void __launch_bounds__(CCL_BX * 8) k_ccl_local_r8(const __grid_constant__ FrameSet fs) { ccl_local_impl<8>(fs); }
-__global__ void __launch_bounds__(CCL_BX * 16) k_ccl_local_r16(const __grid_constant__ FrameSet fs) { ccl_local_impl<16>(fs); }
-__global__ void __launch_bounds__(CCL_BX * 32) k_ccl_local_r32(const __grid_constant__ FrameSet fs) { ccl_local_impl<32>(fs); }
+__global__ void __launch_bounds__(CCL_BX * 8, 8) k_ccl_local_r8(const __grid_constant__ FrameSet fs) { ccl_local_impl<8>(fs); }
+__global__ void __launch_bounds__(CCL_BX * 16, 4) k_ccl_local_r16(const __grid_constant__ FrameSet fs) { ccl_local_impl<16>(fs); }
+__global__ void __launch_bounds__(CCL_BX * 32, 2) k_ccl_local_r32(const __grid_constant__ FrameSet fs) { ccl_local_impl<32>(fs); }
 __global__ void __launch_bounds__(256) k_ccl_border_r8(const __grid_constant__ FrameSet fs) { ccl_border_impl<8>(fs); }
 __global__ void __launch_bounds__(256) k_ccl_border_r16(const __grid_constant__ FrameSet fs) { ccl_border_impl<16>(fs); }
 __global__ void __launch_bounds__(256) k_ccl_border_r32(const __grid_constant__ FrameSet fs) { ccl_border_impl<32>(fs); }
+__global__ void __launch_bounds__(256) k_ccl_border_edges_r8(const __grid_constant__ FrameSet fs) { ccl_border_edges_impl<8>(fs); }
+__global__ void __launch_bounds__(256) k_ccl_border_edges_r16(const __grid_constant__ FrameSet fs) { ccl_border_edges_impl<16>(fs); }
+__global__ void __launch_bounds__(256) k_ccl_border_edges_r32(const __grid_constant__ FrameSet fs) { ccl_border_edges_impl<32>(fs); }
 
 }  // namespace atag
