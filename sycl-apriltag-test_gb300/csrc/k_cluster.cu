@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(256) k_reset_frames(const __grid_constant__ Fr
 // 1. boundaries + per-pair aggregation
 // ---------------------------------------------------------------------------
 constexpr int BP_W = 64;                       // tile width; BP_H (8 or 16) rows is a tuning choice
-constexpr int BP_SW = BP_W + 2;
+constexpr int BP_SW = BP_W + 8;  // label row: x0 - 4 .. x0 + BP_W + 3 (16-byte aligned body)
 constexpr int BP_LC = 64;                      // CTA hash-table entries (a tile has a few dozen pairs; more go straight to the frame's table)
 constexpr uint32_t BP_VALUE = 0x3FFFFFFFu;  // label value without the colour bit
 
@@ -112,14 +112,15 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     uint32_t* status = F.counters + CNT_STATUS;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-    // labels of the tile and its halo (column 0 = x0 - 1, BP_W + 1 = x0 +
-    // BP_W; row BP_H is the row below the tile), and three bit planes of
+    // labels of the tile and its halo (column c = pixel x0 + c - 4: 3 = x0 -
+    // 1, BP_W + 4 = x0 + BP_W; row BP_H is the row below the tile), and
+    // three bit planes of
     // them: per row four words, [0] bit 31 = x0 - 1, [1] and [2] = x0 ..
     // x0 + 63, [3] bit 0 = x0 + 64.  Plane 0: the colour bit (255 pixel),
     // 1: the component has at least min_size pixels, 2: the label is one of
     // the two labels of the frame's first pair known to be over the cluster
     // size limit.
-    __shared__ uint32_t lab[BP_SH][BP_SW];
+    __shared__ __align__(16) uint32_t lab[BP_SH][BP_SW];
     __shared__ __align__(16) uint32_t planes[3][BP_SH][4];
     __shared__ PairTableSmem T;
     __shared__ uint32_t stage[BP_STAGE];
@@ -127,14 +128,11 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     const bool track_dead = !F.stage_outputs && F.dead_pairs;
 
     // pairs that earlier tiles already pushed over the cluster size limit
-    // (a snapshot per warp: a pair published later is simply processed in
-    // full; points of a published pair can never survive, so warps that
-    // see different snapshots still agree on the result)
-    unsigned long long dk0 = EMPTY_KEY, dk1 = EMPTY_KEY;
-    if (track_dead) {
-        dk0 = __ldcg(F.dead_pairs);
-        dk1 = __ldcg(F.dead_pairs + 1);
-    }
+    // (snapshots: a pair published later is simply processed in full;
+    // points of a published pair can never survive, so steps and warps that
+    // see different snapshots still agree on the result).  The first one
+    // filters points at emission.
+    const unsigned long long dk0 = track_dead ? __ldcg(F.dead_pairs) : EMPTY_KEY;
     // a pair joins a white label (colour bit | an even root slot) and a
     // black one (an odd root slot, or label 0 of pixels that are neither 0
     // nor 255)
@@ -155,46 +153,67 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
         T.gx[i] = 0; T.gy[i] = 0; T.pxgx[i] = 0; T.gslot[i] = INVALID;
     }
-    // Loads: unit u < 2 BP_SH is a 32-pixel word of a row (one label per
-    // lane, coalesced), 2 BP_SH and 2 BP_SH + 1 are the left and right halo
-    // columns (lane = row).  Labels out of the image are 0, as the
-    // reference reads them.  All loads of a warp are issued before its size
-    // gathers, and the planes come from ballots.
+    // Loads.  Unit u < (BP_SH + 1) / 2 is a pair of rows 2u, 2u + 1: lane
+    // (row half, q) loads the four labels x0 + 4q .. + 3 with one 16-byte
+    // load and gathers their sizes; the planes' nibbles are OR-reduced over
+    // the 8 lanes of each 32-pixel word by shuffles.  The last two units are
+    // the left and right halo columns (lane = row).  Labels out of the image
+    // are 0, as the reference reads them (w is a multiple of 4, so a group
+    // of four is in or out as a whole).
     {
-        constexpr int NU = 2 * BP_SH + 2, PER = (NU + NW - 1) / NW;
-        uint32_t v[PER];
-#pragma unroll
-        for (int j = 0; j < PER; j++) {
-            const int u = warp + NW * j;
-            int x = -1, y = h;
-            if (u < 2 * BP_SH) {
-                x = x0 + 32 * (u & 1) + lane;
-                y = y0 + (u >> 1);
-            } else if (u < NU && lane < BP_SH) {
-                x = (u & 1) ? x0 + BP_W : x0 - 1;
-                y = y0 + lane;
-            }
-            v[j] = (x >= 0 && x < w && y < h) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
-        }
+        constexpr int NR = (BP_SH + 1) / 2, NU = NR + 2, PER = (NU + NW - 1) / NW;
+        const int q = lane & 15;
 #pragma unroll
         for (int j = 0; j < PER; j++) {
             const int u = warp + NW * j;
             if (u >= NU) break;
-            const uint32_t lv = v[j];
-            const unsigned pc = __ballot_sync(FULL, lv & LABEL_PIXEL_MASK);
-            const unsigned pb = __ballot_sync(FULL, __ldg(F.sizes + (lv & LABEL_VALUE_MASK)) >= min_size);
-            const unsigned pd = __ballot_sync(FULL, lv == dW || lv == dK);
-            if (u < 2 * BP_SH) {
-                const int r = u >> 1, q = 1 + (u & 1);
-                lab[r][q == 1 ? 1 + lane : 33 + lane] = lv;
-                if (lane < 3) planes[lane][r][q] = lane == 0 ? pc : (lane == 1 ? pb : pd);
-            } else if (lane < BP_SH) {
-                const bool right = u & 1;
-                lab[lane][right ? BP_W + 1 : 0] = lv;
-                const int q = right ? 3 : 0, sh = right ? 0 : 31;
-                planes[0][lane][q] = ((pc >> lane) & 1u) << sh;
-                planes[1][lane][q] = ((pb >> lane) & 1u) << sh;
-                planes[2][lane][q] = ((pd >> lane) & 1u) << sh;
+            if (u < NR) {
+                const int r = 2 * u + (lane >> 4), y = y0 + r, x = x0 + 4 * q;
+                const bool in = r < BP_SH && y < h && x < w;
+                const uint4 lv = in ? __ldg(reinterpret_cast<const uint4*>(F.labels + (size_t)y * w + x))
+                                    : make_uint4(0u, 0u, 0u, 0u);
+                const uint32_t l4[4] = {lv.x, lv.y, lv.z, lv.w};
+                uint32_t sz[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) sz[e] = __ldg(F.sizes + (l4[e] & LABEL_VALUE_MASK));
+                uint32_t nc = 0, nbg = 0, nd = 0;
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    nc |= (l4[e] >> 31) << e;
+                    nbg |= (sz[e] >= min_size ? 1u : 0u) << e;
+                    nd |= (l4[e] == dW || l4[e] == dK ? 1u : 0u) << e;
+                }
+                const int sh = 4 * (q & 7);
+                nc <<= sh;
+                nbg <<= sh;
+                nd <<= sh;
+#pragma unroll
+                for (int o = 1; o < 8; o <<= 1) {
+                    nc |= __shfl_xor_sync(FULL, nc, o);
+                    nbg |= __shfl_xor_sync(FULL, nbg, o);
+                    nd |= __shfl_xor_sync(FULL, nd, o);
+                }
+                if (r < BP_SH) {
+                    *reinterpret_cast<uint4*>(&lab[r][4 + 4 * q]) = lv;
+                    if ((q & 7) == 0) {
+                        const int wq = 1 + (q >> 3);
+                        planes[0][r][wq] = nc;
+                        planes[1][r][wq] = nbg;
+                        planes[2][r][wq] = nd;
+                    }
+                }
+            } else {
+                const bool right = u == NR + 1;
+                const int x = right ? x0 + BP_W : x0 - 1, y = y0 + lane;
+                const uint32_t lv = (lane < BP_SH && x >= 0 && x < w && y < h) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
+                const bool bg = __ldg(F.sizes + (lv & LABEL_VALUE_MASK)) >= min_size;
+                if (lane < BP_SH) {
+                    lab[lane][right ? BP_W + 4 : 3] = lv;
+                    const int wq = right ? 3 : 0, sh = right ? 0 : 31;
+                    planes[0][lane][wq] = (lv >> 31) << sh;
+                    planes[1][lane][wq] = (bg ? 1u : 0u) << sh;
+                    planes[2][lane][wq] = (lv == dW || lv == dK ? 1u : 0u) << sh;
+                }
             }
         }
     }
@@ -262,6 +281,12 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         if (lane == 0 && nall_w) atomicAdd(&s_nall, nall_w);
     }
     __syncwarp();
+    // the over-limit pairs again, for the rounds (a later snapshot)
+    unsigned long long dead0 = EMPTY_KEY, dead1 = EMPTY_KEY;
+    if (track_dead) {
+        dead0 = __ldcg(F.dead_pairs);
+        dead1 = __ldcg(F.dead_pairs + 1);
+    }
     // The warp takes its staged points 32 at a time: pair key, CTA table
     // slot (one insert per distinct key of the round) and the per-pair sums
     // of the round's points, merged into the table by one lane per key.
@@ -269,7 +294,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         const uint32_t i = b0 + (uint32_t)lane;
         const bool v = i < nst;
         uint32_t e = v ? wst[i] : 0u;
-        const int xo = (int)(e & 63), ro = (int)((e >> 6) & 15), t = (int)((e >> 10) & 3), c = xo + 1;
+        const int xo = (int)(e & 63), ro = (int)((e >> 6) & 15), t = (int)((e >> 10) & 3), c = xo + 4;
         const int rr = ro + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
         const uint32_t p = lab[ro][c], q = lab[rr][cc];
         const uint32_t lp = p & BP_VALUE, lq = q & BP_VALUE;
@@ -278,7 +303,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         // a round whose points all belong to pairs already over the limit
         // contributes nothing: its points are neither aggregated nor listed
         static_assert(DEAD_PAIRS == 2, "the test below reads both entries");
-        const bool dead = v && (key == dk0 || key == dk1);
+        const bool dead = v && (key == dead0 || key == dead1);
         if (__all_sync(0xFFFFFFFFu, dead || !v)) {
             if (v) wst[i] = e | STAGE_DIRECT;
             continue;
