@@ -65,15 +65,20 @@ struct PairTableSmem {
 };
 
 // Insert-or-find in the CTA's pair table; a plain read first avoids the
-// atomic for keys that are already present (the common case).
-__device__ __forceinline__ int local_insert(PairTableSmem& T, unsigned long long key) {
+// atomic for keys that are already present (the common case).  *fresh is
+// set when this call inserted the key.
+__device__ __forceinline__ int local_insert(PairTableSmem& T, unsigned long long key, bool* fresh) {
     uint32_t h = hash_key(key) & (BP_LC - 1);
     for (int p = 0; p < BP_LC; p++) {
         unsigned long long k = *(volatile unsigned long long*)&T.key[h];
         if (k == key) return (int)h;
         if (k == EMPTY_KEY) {
             k = atomicCAS(&T.key[h], EMPTY_KEY, key);
-            if (k == EMPTY_KEY || k == key) return (int)h;
+            if (k == EMPTY_KEY) {
+                *fresh = true;
+                return (int)h;
+            }
+            if (k == key) return (int)h;
         }
         h = (h + 1) & (BP_LC - 1);
     }
@@ -311,7 +316,17 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         const unsigned m = __match_any_sync(0xFFFFFFFFu, key);
         const int leader = __ffs(m) - 1;
         int ls = 0;
-        if (v && lane == leader) ls = local_insert(T, key);
+        if (v && lane == leader) {
+            // a key new to the tile also takes its slot in the frame's
+            // table now, so the merge below needs one round trip less
+            bool fresh = false;
+            ls = local_insert(T, key, &fresh);
+            if (fresh) {
+                const uint32_t gs = global_insert(F, key);
+                if (gs == INVALID) atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
+                T.gslot[ls] = gs;
+            }
+        }
         ls = __shfl_sync(0xFFFFFFFFu, ls, leader);
         const uint32_t xd = 2u * (uint32_t)(x0 + xo) + 1u, yd = 2u * (uint32_t)(y0 + ro);
         const int gx = dir ? 1 : -1;
@@ -358,12 +373,8 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
         unsigned long long key = T.key[i];
         if (key == EMPTY_KEY) continue;
-        uint32_t gs = global_insert(F, key);
-        if (gs == INVALID) {
-            atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
-            T.gslot[i] = INVALID;
-            continue;
-        }
+        const uint32_t gs = T.gslot[i];  // INVALID: the frame's table was full (flagged)
+        if (gs == INVALID) continue;
         uint32_t old = global_flush(F, gs, T.cnt[i], T.xmin[i], T.xmax[i], T.ymin[i], T.ymax[i], T.gx[i], T.gy[i],
                                     T.pxgx[i]);
         T.gslot[i] = (old + T.cnt[i] > max_pixels) ? INVALID : gs;
