@@ -14,7 +14,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("ATAG_REFERENCE_TREE", "/root/reference")
+# the reference tree: ATAG_REFERENCE_TREE, else a checkout named "reference"
+# beside this repository
+REF = os.environ.get("ATAG_REFERENCE_TREE") or os.path.normpath(
+    os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference"))
 OUT_DIR = os.path.join(HERE, "..", "_ref")
 BIN = os.path.join(OUT_DIR, "refshim_harness")
 REF_SOURCES = ["threshold.cpp", "segmentation.cpp", "find_boundaries.cpp", "fit_quad.cpp"]

@@ -35,7 +35,10 @@ sys.path.insert(0, os.path.join(ROOT, "sycl-apriltag-test_gb300"))
 
 import golden_io  # noqa: E402
 
-REF = os.environ.get("ATAG_REFERENCE_TREE", "/root/reference")
+# the reference tree: ATAG_REFERENCE_TREE, else a checkout named "reference"
+# beside this repository
+REF = os.environ.get("ATAG_REFERENCE_TREE") or os.path.normpath(
+    os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "..", "..", "reference"))
 
 
 def small_frames():
