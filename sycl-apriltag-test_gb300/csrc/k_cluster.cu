@@ -122,11 +122,11 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     // three bit planes of
     // them: per row four words, [0] bit 31 = x0 - 1, [1] and [2] = x0 ..
     // x0 + 63, [3] bit 0 = x0 + 64.  Plane 0: the colour bit (255 pixel),
-    // 1: the component has at least min_size pixels, 2: the label is one of
-    // the two labels of the frame's first pair known to be over the cluster
-    // size limit.
+    // 1: the component has at least min_size pixels, 2 and 3: the label is
+    // one of the two labels of the frame's first / second pair known to be
+    // over the cluster size limit.
     __shared__ __align__(16) uint32_t lab[BP_SH][BP_SW];
-    __shared__ __align__(16) uint32_t planes[3][BP_SH][4];
+    __shared__ __align__(16) uint32_t planes[4][BP_SH][4];
     __shared__ PairTableSmem T;
     __shared__ uint32_t stage[BP_STAGE];
     __shared__ uint32_t s_nall;
@@ -135,23 +135,27 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     // pairs that earlier tiles already pushed over the cluster size limit
     // (snapshots: a pair published later is simply processed in full;
     // points of a published pair can never survive, so steps and warps that
-    // see different snapshots still agree on the result).  The first one
-    // filters points at emission.
-    const unsigned long long dk0 = track_dead ? __ldcg(F.dead_pairs) : EMPTY_KEY;
+    // see different snapshots still agree on the result).  Both filter
+    // points at emission.
+    static_assert(DEAD_PAIRS == 2, "two over-limit pair planes");
     // a pair joins a white label (colour bit | an even root slot) and a
     // black one (an odd root slot, or label 0 of pixels that are neither 0
-    // nor 255)
-    uint32_t dW = FULL, dK = FULL;
-    {
-        const uint32_t kA = (uint32_t)(dk0 >> 32), kB = (uint32_t)dk0;
+    // nor 255): its two label words
+    auto pair_labels = [&](unsigned long long key, uint32_t& lw, uint32_t& lk) {
+        lw = FULL;
+        lk = FULL;
+        const uint32_t kA = (uint32_t)(key >> 32), kB = (uint32_t)key;
         if ((kA ^ kB) & 1u) {
-            dW = LABEL_PIXEL_MASK | ((kA & 1u) ? kB : kA);
-            dK = (kA & 1u) ? kA : kB;
+            lw = LABEL_PIXEL_MASK | ((kA & 1u) ? kB : kA);
+            lk = (kA & 1u) ? kA : kB;
         } else if (kA == 0u) {
-            dW = LABEL_PIXEL_MASK | kB;
-            dK = 0u;
+            lw = LABEL_PIXEL_MASK | kB;
+            lk = 0u;
         }
-    }
+    };
+    uint32_t dW, dK, eW, eK;
+    pair_labels(track_dead ? __ldcg(F.dead_pairs) : EMPTY_KEY, dW, dK);
+    pair_labels(track_dead ? __ldcg(F.dead_pairs + 1) : EMPTY_KEY, eW, eK);
     if (threadIdx.x == 0) s_nall = 0;
     for (int i = threadIdx.x; i < BP_LC; i += blockDim.x) {
         T.key[i] = EMPTY_KEY;
@@ -181,22 +185,25 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
                 uint32_t sz[4];
 #pragma unroll
                 for (int e = 0; e < 4; e++) sz[e] = __ldg(F.sizes + (l4[e] & LABEL_VALUE_MASK));
-                uint32_t nc = 0, nbg = 0, nd = 0;
+                uint32_t nc = 0, nbg = 0, nd = 0, ne = 0;
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
                     nc |= (l4[e] >> 31) << e;
                     nbg |= (sz[e] >= min_size ? 1u : 0u) << e;
                     nd |= (l4[e] == dW || l4[e] == dK ? 1u : 0u) << e;
+                    ne |= (l4[e] == eW || l4[e] == eK ? 1u : 0u) << e;
                 }
                 const int sh = 4 * (q & 7);
                 nc <<= sh;
                 nbg <<= sh;
                 nd <<= sh;
+                ne <<= sh;
 #pragma unroll
                 for (int o = 1; o < 8; o <<= 1) {
                     nc |= __shfl_xor_sync(FULL, nc, o);
                     nbg |= __shfl_xor_sync(FULL, nbg, o);
                     nd |= __shfl_xor_sync(FULL, nd, o);
+                    ne |= __shfl_xor_sync(FULL, ne, o);
                 }
                 if (r < BP_SH) {
                     *reinterpret_cast<uint4*>(&lab[r][4 + 4 * q]) = lv;
@@ -205,6 +212,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
                         planes[0][r][wq] = nc;
                         planes[1][r][wq] = nbg;
                         planes[2][r][wq] = nd;
+                        planes[3][r][wq] = ne;
                     }
                 }
             } else {
@@ -218,6 +226,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
                     planes[0][lane][wq] = (lv >> 31) << sh;
                     planes[1][lane][wq] = (bg ? 1u : 0u) << sh;
                     planes[2][lane][wq] = (lv == dW || lv == dK ? 1u : 0u) << sh;
+                    planes[3][lane][wq] = (lv == eW || lv == eK ? 1u : 0u) << sh;
                 }
             }
         }
@@ -245,27 +254,32 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
             L = __funnelshift_l(prev, C, 1);  // bit i: pixel xb + i - 1
             R = __funnelshift_r(C, next, 1);  // bit i: pixel xb + i + 1
         };
-        uint32_t c0L, c0, c0R, b0L, b0, b0R, d0L, d0, d0R;
+        uint32_t c0L, c0, c0R, b0L, b0, b0R;
         word(0, r, c0L, c0, c0R);
         word(1, r, b0L, b0, b0R);
-        word(2, r, d0L, d0, d0R);
         uint32_t live = (y0 + r < h) ? (xb + 32 <= w ? FULL : (xb < w ? ((1u << (w - xb)) - 1u) : 0u)) : 0u;
         if (xb == 0) live &= ~1u;  // column 0 is never processed
         live &= b0 & (half ? 0xFFFF0000u : 0x0000FFFFu);
         // the tested neighbour of test t: R (x + 1, y), BL (x - 1, y + 1),
         // B (x, y + 1), BR (x + 1, y + 1)
-        uint32_t nc = c0R, nbg = b0R, nd = d0R;
-        uint32_t c1L, c1, c1R, b1L, b1, b1R, d1L, d1, d1R;
+        uint32_t nc = c0R, nbg = b0R;
+        uint32_t c1L, c1, c1R, b1L, b1, b1R;
         word(0, r + 1, c1L, c1, c1R);
         word(1, r + 1, b1L, b1, b1R);
-        word(2, r + 1, d1L, d1, d1R);
-        if (t == 1) { nc = c1L; nbg = b1L; nd = d1L; }
-        if (t == 2) { nc = c1; nbg = b1; nd = d1; }
-        if (t == 3) { nc = c1R; nbg = b1R; nd = d1R; }
+        if (t == 1) { nc = c1L; nbg = b1L; }
+        if (t == 2) { nc = c1; nbg = b1; }
+        if (t == 3) { nc = c1R; nbg = b1R; }
         // BL is not emitted where the left pixel's BR covers the same pair
         const uint32_t keep = t == 1 ? ~((c0L ^ c1) & b0L & b1) : FULL;
         mt = (nc ^ c0) & nbg & live & keep;
-        st = mt & ~(d0 & nd);
+        // points whose two pixels are both labels of one published pair
+        auto of_pair = [&](int p) {
+            uint32_t L0, C0, R0, L1, C1, R1;
+            word(p, r, L0, C0, R0);
+            word(p, r + 1, L1, C1, R1);
+            return C0 & (t == 0 ? R0 : (t == 1 ? L1 : (t == 2 ? C1 : R1)));
+        };
+        st = mt & ~(of_pair(2) | of_pair(3));
     }
     // Each warp lists its staged points in its own part of the staging
     // array (warp scan) and aggregates them itself, so no CTA barrier
