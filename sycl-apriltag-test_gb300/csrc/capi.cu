@@ -104,6 +104,10 @@ dim3 grid2(size_t x, size_t y) {
     return dim3((unsigned)x, (unsigned)y);
 }
 size_t cdiv(size_t a, size_t b) { return (a + b - 1) / b; }
+// tile CCL grid: (tile columns, tile rows, frames) of the largest frame
+dim3 ccl_grid(size_t w, size_t h, size_t rows, size_t frames) {
+    return dim3((unsigned)cdiv(w / 2, 32), (unsigned)cdiv(h / 2, rows), (unsigned)frames);
+}
 
 FrameSet single(const FrameDesc& d) {
     FrameSet s;
@@ -437,12 +441,12 @@ static atag_status launch_segmentation(const FrameSet& fs, size_t max_w, size_t 
     size_t tiles = cdiv(max_w / 2, 32) * cdiv(max_h / 2, (size_t)rows);
     size_t border = tiles * (32 + 2 * (rows - 1));
     if (rows == 8) {
-        k_ccl_local_r8<<<grid2(tiles, nf), 32 * 8, 0, s>>>(fs);
+        k_ccl_local_r8<<<ccl_grid(max_w, max_h, 8, nf), 32 * 8, 0, s>>>(fs);
         LAUNCHED();
         k_ccl_border_r8<<<grid2(cdiv(border, 256), nf), 256, 0, s>>>(fs);
         LAUNCHED();
     } else {
-        k_ccl_local_r16<<<grid2(tiles, nf), 32 * 16, 0, s>>>(fs);
+        k_ccl_local_r16<<<ccl_grid(max_w, max_h, 16, nf), 32 * 16, 0, s>>>(fs);
         LAUNCHED();
         k_ccl_border_r16<<<grid2(cdiv(border, 256), nf), 256, 0, s>>>(fs);
         LAUNCHED();
@@ -918,9 +922,9 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
     k_threshold<<<grid2(cdiv(mw / 4, 32) * cdiv(mh / 4, 16), n), 256, 0, s>>>(fs, p.min_white_black_diff, 0);
     LAUNCHED();
     STAGE(3);
-    if (ccl_rows == 8) k_ccl_local_r8<<<grid2(tiles_ccl, n), 32 * 8, 0, s>>>(fs);
-    else if (ccl_rows == 32) k_ccl_local_r32<<<grid2(tiles_ccl, n), 32 * 32, 0, s>>>(fs);
-    else k_ccl_local_r16<<<grid2(tiles_ccl, n), 32 * 16, 0, s>>>(fs);
+    if (ccl_rows == 8) k_ccl_local_r8<<<ccl_grid(mw, mh, 8, n), 32 * 8, 0, s>>>(fs);
+    else if (ccl_rows == 32) k_ccl_local_r32<<<ccl_grid(mw, mh, 32, n), 32 * 32, 0, s>>>(fs);
+    else k_ccl_local_r16<<<ccl_grid(mw, mh, 16, n), 32 * 16, 0, s>>>(fs);
     LAUNCHED();
     STAGE(4);
     {
@@ -934,12 +938,12 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
     k_ccl_final<<<grid2(std::min<size_t>(cdiv((mw / 4) * (mh / 2), 256), 8192), n), 256, 0, s>>>(fs);
     LAUNCHED();
     STAGE(6);
-    // grid (frames, tiles): at most 64 x 512 tiles of a 4096 x 4096 frame,
-    // within gridDim.y's 65535
+    // grid (frames, tile columns, tile rows): at most 64 x 512 tiles of a
+    // 4096 x 4096 frame
     if (bp_rows == 8)
-        k_boundaries_pairs_r8<<<dim3((unsigned)n, (unsigned)(cdiv(mw, 64) * cdiv(mh, 8))), 16 * 8, 0, s>>>(fs, p.min_component_size);
+        k_boundaries_pairs_r8<<<dim3((unsigned)n, (unsigned)cdiv(mw, 64), (unsigned)cdiv(mh, 8)), 16 * 8, 0, s>>>(fs, p.min_component_size);
     else
-        k_boundaries_pairs_r16<<<dim3((unsigned)n, (unsigned)(cdiv(mw, 64) * cdiv(mh, 16))), 16 * 16, 0, s>>>(fs, p.min_component_size);
+        k_boundaries_pairs_r16<<<dim3((unsigned)n, (unsigned)cdiv(mw, 64), (unsigned)cdiv(mh, 16)), 16 * 16, 0, s>>>(fs, p.min_component_size);
     LAUNCHED();
     STAGE(7);
     k_pairs_finalize<<<(unsigned)n, 1024, 0, s>>>(fs, p, (uint32_t)tu.small_cluster_max);

@@ -105,15 +105,15 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     constexpr int BP_WSTAGE = 2 * BP_W * 4;    // the part of one warp (two tile rows)
     constexpr unsigned FULL = 0xFFFFFFFFu;
     static_assert(BP_W == 64, "two 32-pixel words per row");
-    // frame from blockIdx.x, tile from blockIdx.y: CTAs are dispatched
-    // frame-fastest, so the tiles in flight at once span every frame of the
-    // batch and a frame's later tiles start after its first ones published
-    // their over-limit pairs
+    // frame from blockIdx.x, tile column and row from blockIdx.y and .z:
+    // CTAs are dispatched frame-fastest, so the tiles in flight at once span
+    // every frame of the batch and a frame's later tiles start after its
+    // first ones published their over-limit pairs
     const FrameDesc& F = fs.get(blockIdx.x);
     const int w = F.width, h = F.height;
     const int ntx = (w + BP_W - 1) / BP_W, nty = (h + BP_H - 1) / BP_H;
-    if ((int)blockIdx.y >= ntx * nty) return;
-    const int x0 = (blockIdx.y % ntx) * BP_W, y0 = (blockIdx.y / ntx) * BP_H;
+    if ((int)blockIdx.y >= ntx || (int)blockIdx.z >= nty) return;
+    const int x0 = blockIdx.y * BP_W, y0 = blockIdx.z * BP_H;
     uint32_t* status = F.counters + CNT_STATUS;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 

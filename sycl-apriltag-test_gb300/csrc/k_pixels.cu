@@ -241,12 +241,15 @@ template <int CCL_BY>
 __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     constexpr int CCL_THREADS = CCL_BX * CCL_BY;
     constexpr unsigned FULL = 0xFFFFFFFFu;
-    const FrameDesc& F = fs.get(blockIdx.y);
+    // grid (tile column, tile row, frame): the frame's tile from the block
+    // indices, no division
+    const FrameDesc& F = fs.get(blockIdx.z);
     const int w = F.width, h = F.height;
     const int ntx = ccl_tiles_x(w), nty = ccl_tiles_y<CCL_BY>(h);
-    if ((int)blockIdx.x >= ntx * nty) return;
-    const int bx0 = (blockIdx.x % ntx) * CCL_BX, by0 = (blockIdx.x / ntx) * CCL_BY;
+    if ((int)blockIdx.x >= ntx || (int)blockIdx.y >= nty) return;
+    const int bx0 = blockIdx.x * CCL_BX, by0 = blockIdx.y * CCL_BY;
     const int x0 = bx0 * 2, y0 = by0 * 2;
+    const uint32_t tile = blockIdx.y * (uint32_t)ntx + blockIdx.x;  // row-major within the frame
 
     constexpr int PH = 2 * CCL_BY + 1, WPR = (2 * CCL_BX + 8) / 4;
     static_assert(WPR <= 32 && PH <= 3 * CCL_BY, "one word per lane, three rows per warp");
@@ -399,7 +402,7 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         // the edge record: tile roots of the edge blocks, with the block's
         // links of that forest in bits 24-27 (slots are below 2^24); links
         // that leave the tile are the border pass's work
-        uint2* rec = reinterpret_cast<uint2*>(F.edges + (size_t)blockIdx.x * ccl_edge_words(CCL_BY));
+        uint2* rec = reinterpret_cast<uint2*>(F.edges + (size_t)tile * ccl_edge_words(CCL_BY));
         const uint32_t lk = s_links[threadIdx.x];
         const uint2 e = make_uint2(parents.x | ((lk & 15u) << 24), parents.y | ((lk >> 4) << 24));
         if (ty == 0) rec[tx] = e;

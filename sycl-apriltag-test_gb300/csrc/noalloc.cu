@@ -78,7 +78,7 @@ extern "C" atag_status atag_image_segmentation_noalloc(const uint8_t* thr, uint3
     d.stage_outputs = 1;  // the reference's sizes array, zeros away from roots
     cudaStream_t s = (cudaStream_t)stream;
     const size_t tiles = ((w / 2 + 31) / 32) * ((h / 2 + 15) / 16);
-    k_ccl_local_r16<<<dim3((unsigned)tiles, 1), 512, 0, s>>>(fs);
+    k_ccl_local_r16<<<dim3((unsigned)((w / 2 + 31) / 32), (unsigned)((h / 2 + 15) / 16), 1), 512, 0, s>>>(fs);
     count_launch();
     k_ccl_border_r16<<<dim3((unsigned)((tiles * (32 + 2 * (16 - 1)) + 255) / 256), 1), 256, 0, s>>>(fs);
     count_launch();
