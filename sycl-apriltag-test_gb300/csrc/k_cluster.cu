@@ -162,73 +162,54 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         T.cnt[i] = 0; T.xmin[i] = 0xFFFFFFFFu; T.xmax[i] = 0; T.ymin[i] = 0xFFFFFFFFu; T.ymax[i] = 0;
         T.gx[i] = 0; T.gy[i] = 0; T.pxgx[i] = 0; T.gslot[i] = INVALID;
     }
-    // Loads.  Unit u < (BP_SH + 1) / 2 is a pair of rows 2u, 2u + 1: lane
-    // (row half, q) loads the four labels x0 + 4q .. + 3 with one 16-byte
-    // load and gathers their sizes; the planes' nibbles are OR-reduced over
-    // the 8 lanes of each 32-pixel word by shuffles.  The last two units are
-    // the left and right halo columns (lane = row).  Labels out of the image
-    // are 0, as the reference reads them (w is a multiple of 4, so a group
-    // of four is in or out as a whole).
+    // Loads.  Row-word unit u = 2 r + k (row r of the tile and its halo row,
+    // 32-pixel word k) belongs to warp u % NW: lane i loads the label of
+    // pixel x0 + 32 k + i (one coalesced 128-byte row segment per warp) and
+    // gathers its component's size, and four warp ballots of the flags are
+    // the unit's four plane words.  The last two warps, which have one unit
+    // fewer, also load the left and right halo columns (lane = row).  A
+    // lane issues all its label loads before the first size gather.  Labels
+    // out of the image are 0, as the reference reads them.
     {
-        constexpr int NR = (BP_SH + 1) / 2, NU = NR + 2, PER = (NU + NW - 1) / NW;
-        const int q = lane & 15;
+        constexpr int NUNIT = 2 * BP_SH, PER = (NUNIT + NW - 1) / NW;
+        static_assert(NUNIT <= NW * (PER - 1) + NW - 2, "the last two warps have a unit fewer");
+        uint32_t lv[PER], sz[PER];
 #pragma unroll
         for (int j = 0; j < PER; j++) {
-            const int u = warp + NW * j;
-            if (u >= NU) break;
-            if (u < NR) {
-                const int r = 2 * u + (lane >> 4), y = y0 + r, x = x0 + 4 * q;
-                const bool in = r < BP_SH && y < h && x < w;
-                const uint4 lv = in ? __ldg(reinterpret_cast<const uint4*>(F.labels + (size_t)y * w + x))
-                                    : make_uint4(0u, 0u, 0u, 0u);
-                const uint32_t l4[4] = {lv.x, lv.y, lv.z, lv.w};
-                uint32_t sz[4];
+            const int u = warp + NW * j, r = u >> 1, x = x0 + 32 * (u & 1) + lane, y = y0 + r;
+            lv[j] = (u < NUNIT && y < h && x < w) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
+        }
+        const bool halo = warp >= NW - 2, right = warp == NW - 1;
+        const int hx = right ? x0 + BP_W : x0 - 1, hy = y0 + lane;
+        const uint32_t hl = (halo && lane < BP_SH && hx >= 0 && hx < w && hy < h) ? __ldg(F.labels + (size_t)hy * w + hx) : 0u;
 #pragma unroll
-                for (int e = 0; e < 4; e++) sz[e] = __ldg(F.sizes + (l4[e] & LABEL_VALUE_MASK));
-                uint32_t nc = 0, nbg = 0, nd = 0, ne = 0;
+        for (int j = 0; j < PER; j++)
+            if (warp + NW * j < NUNIT) sz[j] = __ldg(F.sizes + (lv[j] & LABEL_VALUE_MASK));
+        const uint32_t hs = halo ? __ldg(F.sizes + (hl & LABEL_VALUE_MASK)) : 0u;
 #pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    nc |= (l4[e] >> 31) << e;
-                    nbg |= (sz[e] >= min_size ? 1u : 0u) << e;
-                    nd |= (l4[e] == dW || l4[e] == dK ? 1u : 0u) << e;
-                    ne |= (l4[e] == eW || l4[e] == eK ? 1u : 0u) << e;
-                }
-                const int sh = 4 * (q & 7);
-                nc <<= sh;
-                nbg <<= sh;
-                nd <<= sh;
-                ne <<= sh;
-#pragma unroll
-                for (int o = 1; o < 8; o <<= 1) {
-                    nc |= __shfl_xor_sync(FULL, nc, o);
-                    nbg |= __shfl_xor_sync(FULL, nbg, o);
-                    nd |= __shfl_xor_sync(FULL, nd, o);
-                    ne |= __shfl_xor_sync(FULL, ne, o);
-                }
-                if (r < BP_SH) {
-                    *reinterpret_cast<uint4*>(&lab[r][4 + 4 * q]) = lv;
-                    if ((q & 7) == 0) {
-                        const int wq = 1 + (q >> 3);
-                        planes[0][r][wq] = nc;
-                        planes[1][r][wq] = nbg;
-                        planes[2][r][wq] = nd;
-                        planes[3][r][wq] = ne;
-                    }
-                }
-            } else {
-                const bool right = u == NR + 1;
-                const int x = right ? x0 + BP_W : x0 - 1, y = y0 + lane;
-                const uint32_t lv = (lane < BP_SH && x >= 0 && x < w && y < h) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
-                const bool bg = __ldg(F.sizes + (lv & LABEL_VALUE_MASK)) >= min_size;
-                if (lane < BP_SH) {
-                    lab[lane][right ? BP_W + 4 : 3] = lv;
-                    const int wq = right ? 3 : 0, sh = right ? 0 : 31;
-                    planes[0][lane][wq] = (lv >> 31) << sh;
-                    planes[1][lane][wq] = (bg ? 1u : 0u) << sh;
-                    planes[2][lane][wq] = (lv == dW || lv == dK ? 1u : 0u) << sh;
-                    planes[3][lane][wq] = (lv == eW || lv == eK ? 1u : 0u) << sh;
-                }
+        for (int j = 0; j < PER; j++) {
+            const int u = warp + NW * j, r = u >> 1, k = u & 1;
+            if (u >= NUNIT) break;
+            const uint32_t l = lv[j];
+            lab[r][4 + 32 * k + lane] = l;
+            const unsigned bc = __ballot_sync(FULL, (int)l < 0);
+            const unsigned bb = __ballot_sync(FULL, sz[j] >= min_size);
+            const unsigned bd = __ballot_sync(FULL, l == dW || l == dK);
+            const unsigned be = __ballot_sync(FULL, l == eW || l == eK);
+            if (lane == 0) {
+                planes[0][r][1 + k] = bc;
+                planes[1][r][1 + k] = bb;
+                planes[2][r][1 + k] = bd;
+                planes[3][r][1 + k] = be;
             }
+        }
+        if (halo && lane < BP_SH) {
+            lab[lane][right ? BP_W + 4 : 3] = hl;
+            const int wq = right ? 3 : 0, sh = right ? 0 : 31;
+            planes[0][lane][wq] = (hl >> 31) << sh;
+            planes[1][lane][wq] = (hs >= min_size ? 1u : 0u) << sh;
+            planes[2][lane][wq] = (hl == dW || hl == dK ? 1u : 0u) << sh;
+            planes[3][lane][wq] = (hl == eW || hl == eK ? 1u : 0u) << sh;
         }
     }
     __syncthreads();

@@ -251,11 +251,10 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     const int x0 = bx0 * 2, y0 = by0 * 2;
     const uint32_t tile = blockIdx.y * (uint32_t)ntx + blockIdx.x;  // row-major within the frame
 
-    constexpr int PH = 2 * CCL_BY + 1, WPR = (2 * CCL_BX + 8) / 4;
-    static_assert(WPR <= 32 && PH <= 3 * CCL_BY, "one word per lane, three rows per warp");
-    // rows y0 - 1 .., words of pixels x0 - 4 .. x0 + 2 CCL_BX + 3 (x0 and w
-    // are multiples of 4): pixel x of a row is byte x - x0 + 4
-    __shared__ uint32_t pixw[PH][WPR];
+    // words of pixels x0 - 4 .. x0 + 2 CCL_BX + 3 of a row (x0 and w are
+    // multiples of 4): pixel x is byte x - x0 + 4
+    constexpr int WPR = (2 * CCL_BX + 8) / 4;
+    static_assert(WPR <= 32, "one word per lane");
     __shared__ uint32_t par[2 * CCL_THREADS];
     __shared__ uint32_t cnt[2 * CCL_THREADS];
     __shared__ uint32_t row_runs[CCL_BY][2];  // S-link ballots of each tile row (255, 0 forest)
@@ -263,9 +262,12 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     __shared__ uint8_t s_links[CCL_THREADS];  // the blocks' links (edge records)
 
     const int tx = threadIdx.x % CCL_BX, ty = threadIdx.x / CCL_BX;  // lane, warp
-    // the tile's pixels plus a one-pixel halo as aligned 32-bit words: warp
-    // ty loads rows ty, ty + CCL_BY (and warp 0 row 2 CCL_BY), one word per
-    // lane; both loads are issued before either is stored
+    // the warp's pixel rows y - 1, y, y + 1 (y = y0 + 2 ty) with a one-pixel
+    // halo as aligned 32-bit words, one per lane (WPR lanes), that the lanes
+    // share by shuffles: no shared-memory staging and no barrier before the
+    // links (the rows between two warps are read by both, from L1)
+    const int o = 2 * tx + 3, wq = o >> 2, sh = (o & 3) * 8;
+    uint32_t vm, v0, v1;
     {
         const uint32_t* thr32 = reinterpret_cast<const uint32_t*>(F.thr);
         const int xw = x0 - 4 + 4 * tx;
@@ -273,22 +275,20 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         uint32_t v[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-            const int row = ty + k * CCL_BY, y = y0 - 1 + row;
-            v[k] = (colok && row < PH && y >= 0 && y < h) ? __ldg(thr32 + (size_t)y * (uint32_t)(w >> 2) + (xw >> 2))
-                                                          : 0x7F7F7F7Fu;
+            const int y = y0 - 1 + 2 * ty + k;
+            v[k] = (colok && y >= 0 && y < h) ? __ldg(thr32 + (size_t)y * (uint32_t)(w >> 2) + (xw >> 2)) : 0x7F7F7F7Fu;
         }
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const int row = ty + k * CCL_BY;
-            if (tx < WPR && row < PH) pixw[row][tx] = v[k];
-        }
+        // pixels x - 1 .. x + 2 of a row as one word (x = 2 bx)
+        auto win = [&](uint32_t r) { return __funnelshift_r(__shfl_sync(FULL, r, wq), __shfl_sync(FULL, r, wq + 1), sh); };
+        vm = win(v[0]);
+        v0 = win(v[1]);
+        v1 = win(v[2]);
     }
     const int bx = bx0 + tx, by = by0 + ty;
     const bool live = bx < w / 2 && by < h / 2;
     const uint32_t l = threadIdx.x;
     cnt[2 * l] = 0;
     cnt[2 * l + 1] = 0;
-    __syncthreads();
 
     // The block's links, computed on bytes: p(x - 1) .. p(x + 2) of pixel
     // rows y - 1, y and y + 1 (x = 2 bx, y = 2 by) as one word each, and
@@ -298,9 +298,6 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     // (up-right) p(x+2, y-1) when TR is, S (left) p(x-1, y) or p(x-1, y+1)
     // when TL or BL is; image edges drop P and S (x = 0), R (x + 2 >= w)
     // and P, Q, R (y = 0).
-    const int o = 2 * tx + 3, wq = o >> 2, sh = (o & 3) * 8;
-    auto win = [&](int row) { return __funnelshift_r(pixw[row][wq], pixw[row][wq + 1], sh); };
-    const uint32_t vm = win(2 * ty), v0 = win(2 * ty + 1), v1 = win(2 * ty + 2);
     const uint32_t Wm = __vcmpeq4(vm, FULL), Km = __vcmpeq4(vm, 0u);
     const uint32_t W0 = __vcmpeq4(v0, FULL), K0 = __vcmpeq4(v0, 0u);
     const uint32_t W1 = __vcmpeq4(v1, FULL), K1 = __vcmpeq4(v1, 0u);
@@ -422,9 +419,7 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
             auto bits = [](uint32_t X0, uint32_t X1) {
                 return ((X0 >> 8) & 1u) | ((X0 >> 15) & 2u) | ((X1 >> 6) & 4u) | ((X1 >> 13) & 8u);
             };
-            const uint32_t u0 = win(2 * ty + 1), u1 = win(2 * ty + 2);  // rows y, y + 1 again
-            *reinterpret_cast<uint2*>(F.scratch + id + w) =
-                make_uint2(bits(__vcmpeq4(u0, FULL), __vcmpeq4(u1, FULL)) | (bits(__vcmpeq4(u0, 0u), __vcmpeq4(u1, 0u)) << 8), 0u);
+            *reinterpret_cast<uint2*>(F.scratch + id + w) = make_uint2(bits(W0, W1) | (bits(K0, K1) << 8), 0u);
         }
     }
 }
