@@ -295,6 +295,43 @@ def run_reference(args, rank):
     print(json.dumps(line))
 
 
+def _serving_runs(cam_frames, W, H, seconds, overload_seconds, device):
+    """The serving runs of the bench, in a process of their own."""
+    sys.path.insert(0, PKG)
+    import torch
+    from atag import serving
+    torch.cuda.set_device(device)
+    slots = serving.executors_for_memory(W, H, 8, 8 * W * H, max_slots=3)
+    rates = [60.0] * 4 + [30.0] * 4
+    # the cameras deliver into pinned capture buffers (no host-side copy)
+    cams = [[torch.from_numpy(f).pin_memory() for f in fr] for fr in cam_frames]
+
+    def run(fn, **kw):
+        srv = serving.Server(slots)
+        serving.warm(srv, cams[4][0])
+        c0 = serving.host_counters()
+        res = fn(srv, cams, **kw)
+        return srv, res, serving.counter_delta(c0, serving.host_counters())
+    srv, res, hc = run(serving.run_cameras, rates_hz=rates, duration_s=seconds, seed=1)
+    line = serving.latency_summary(res, seconds)
+    line.update({"cameras": "4x1280x720@60 + 4x1920x1080@30", "slots": len(slots), "seconds": seconds,
+                 "max_in_flight": srv.max_in_flight, "max_host_stall_ms": 1000.0 * srv.max_poll_gap,
+                 "max_poll_ms": 1000.0 * srv.max_poll_time, "host": hc, "process": "spawned child"})
+    if overload_seconds > 0:
+        srv, res, hc = run(serving.run_cameras, rates_hz=[16 * r for r in rates], duration_s=overload_seconds, seed=2)
+        ov = serving.latency_summary(res, overload_seconds)
+        ov.update({"cameras": "4x1280x720@960 + 4x1920x1080@480", "seconds": overload_seconds,
+                   "max_in_flight": srv.max_in_flight, "max_host_stall_ms": 1000.0 * srv.max_poll_gap,
+                   "max_poll_ms": 1000.0 * srv.max_poll_time, "host": hc})
+        line["overload_16x"] = ov
+        srv, res, hc = run(serving.run_bursts, n_bursts=100, burst_size=16, period_s=0.02)
+        bu = serving.latency_summary(res, 2.0)
+        bu.update({"bursts": "100 bursts of 16 requests, one every 20 ms", "max_in_flight": srv.max_in_flight,
+                   "host": hc})
+        line["bursts_16"] = bu
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -702,37 +739,14 @@ def main():
     # --- serving: 8 cameras (4 x 720p60, 4 x 1080p30), Poisson arrivals;
     # then the same cameras at 16x their rates (more requests than one
     # launch per request keeps up with: they batch), and bursts of 16
-    # simultaneous requests
+    # simultaneous requests.  A server is a process of its own: the runs go
+    # to a spawned child process, away from this process's batch detectors,
+    # graphs and pinned buffers.
     serving_line = None
     if cam_frames:
-        from atag import serving
-        slots = serving.executors_for_memory(W, H, 8, 8 * W * H, max_slots=3)
-        rates = [60.0] * 4 + [30.0] * 4
-        # the cameras deliver into pinned capture buffers (no host-side copy)
-        cam_frames = [[torch.from_numpy(f).pin_memory() for f in fr] for fr in cam_frames]
-
-        def run(fn, **kw):
-            srv = serving.Server(slots)
-            serving.warm(srv, cam_frames[4][0])
-            res = fn(srv, cam_frames, **kw)
-            return srv, res
-        srv, res = run(serving.run_cameras, rates_hz=rates, duration_s=args.serving_seconds, seed=1)
-        serving_line = serving.latency_summary(res, args.serving_seconds)
-        serving_line.update({"cameras": "4x1280x720@60 + 4x1920x1080@30", "slots": len(slots),
-                             "seconds": args.serving_seconds, "max_in_flight": srv.max_in_flight,
-                             "max_host_stall_ms": 1000.0 * srv.max_poll_gap})
-        if args.overload_seconds > 0:
-            srv, res = run(serving.run_cameras, rates_hz=[16 * r for r in rates], duration_s=args.overload_seconds,
-                           seed=2)
-            ov = serving.latency_summary(res, args.overload_seconds)
-            ov.update({"cameras": "4x1280x720@960 + 4x1920x1080@480", "seconds": args.overload_seconds,
-                       "max_in_flight": srv.max_in_flight, "max_host_stall_ms": 1000.0 * srv.max_poll_gap})
-            serving_line["overload_16x"] = ov
-            srv, res = run(serving.run_bursts, n_bursts=100, burst_size=16, period_s=0.02)
-            bu = serving.latency_summary(res, 2.0)
-            bu.update({"bursts": "100 bursts of 16 requests, one every 20 ms", "max_in_flight": srv.max_in_flight})
-            serving_line["bursts_16"] = bu
-        del slots, srv
+        with concurrent.futures.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
+            serving_line = pool.submit(_serving_runs, cam_frames, W, H, args.serving_seconds,
+                                       args.overload_seconds, local_rank).result()
 
     # --- CPU baseline (rank 0, N=1)
     cpu = None

@@ -18,6 +18,7 @@ with a fake executor and run on the GPU with DetectorExecutor.
 import collections
 import contextlib
 import gc
+import resource
 import time
 from dataclasses import dataclass, field
 
@@ -159,6 +160,7 @@ class Server:
         self.completed = []
         self.max_in_flight = 0
         self.max_poll_gap = 0.0  # longest time between two polls (host stalls)
+        self.max_poll_time = 0.0  # longest single poll (launches, result copies, stalls inside it)
         self._last_poll = None
 
     def now(self):
@@ -201,9 +203,14 @@ class Server:
         self._reap()
         self._admit()
         self._last_poll = self.clock()
+        self.max_poll_time = max(self.max_poll_time, self._last_poll - t)
 
     def idle(self):
         return not self.queue and all(b is None for b in self.busy)
+
+    def mark_resumed(self):
+        """After a deliberate sleep: the gap since the last poll is not a stall."""
+        self._last_poll = self.clock()
 
     def drain(self, timeout_s=60.0):
         end = self.now() + timeout_s
@@ -236,16 +243,43 @@ def poisson_arrivals(rates_hz, duration_s, seed):
 @contextlib.contextmanager
 def latency_critical():
     """For the length of a serving run: one full garbage collection up front,
-    then the objects that exist are frozen out of the collector's reach, so
-    the collections that run during the loop only scan what the loop itself
-    allocates (a full collection over a large process can stall the loop
-    for milliseconds)."""
+    then automatic collection off until the run ends.  The loop allocates a
+    result record per request; with the collector on, its oldest generation
+    is collected every so often over all the results kept so far, which in a
+    minute-long run stalled a poll for up to ~60 ms (inside `poll`, so the
+    gap between polls did not show it).  The objects that exist before the
+    run are also frozen, so the collection after it skips them."""
     gc.collect()
     gc.freeze()
+    gc.disable()
     try:
         yield
     finally:
+        gc.enable()
         gc.unfreeze()
+
+
+def host_counters():
+    """Host-side counters that explain stalls of the request loop: this
+    process's involuntary context switches (the scheduler took the CPU away)
+    and, where the cgroup exposes them, the times the process's CPU quota
+    was exhausted and its threads throttled."""
+    out = {"involuntary_switches": resource.getrusage(resource.RUSAGE_SELF).ru_nivcsw}
+    for path in ("/sys/fs/cgroup/cpu.stat", "/sys/fs/cgroup/cpu/cpu.stat", "/sys/fs/cgroup/cpu,cpuacct/cpu.stat"):
+        try:
+            with open(path) as f:
+                for line in f:
+                    k, _, v = line.partition(" ")
+                    if k in ("nr_throttled", "throttled_usec", "throttled_time"):
+                        out["cgroup_" + k] = int(v)
+            break
+        except (OSError, ValueError):
+            continue
+    return out
+
+
+def counter_delta(before, after):
+    return {k: after[k] - before[k] for k in after if k in before}
 
 
 def warm(server: Server, frame):
@@ -256,10 +290,14 @@ def warm(server: Server, frame):
         ex.results()
 
 
-def run_cameras(server: Server, camera_frames, rates_hz, duration_s, seed=0, on_result=None):
+def run_cameras(server: Server, camera_frames, rates_hz, duration_s, seed=0, on_result=None, idle_sleep=True):
     """Replays Poisson arrivals in real time: camera c submits
     camera_frames[c][k % len] at each of its arrival times.  Returns the
-    completed results sorted by sequence number."""
+    completed results sorted by sequence number.  With idle_sleep, the loop
+    sleeps while nothing is queued or in flight until shortly before the
+    next arrival instead of spinning, so it holds a CPU only while it has
+    work (a loop that spins all the time is the first thread a busy host
+    preempts)."""
     arrivals = poisson_arrivals(rates_hz, duration_s, seed)
     counters = collections.Counter()
     seq = 0
@@ -267,8 +305,14 @@ def run_cameras(server: Server, camera_frames, rates_hz, duration_s, seed=0, on_
     with latency_critical():
         server.t0 = server.clock()
         while i < len(arrivals):
-            while server.now() < arrivals[i][0]:
+            while True:
+                wait = arrivals[i][0] - server.now()
+                if wait <= 0:
+                    break
                 server.poll()
+                if idle_sleep and wait > 3e-4 and server.idle():
+                    time.sleep(wait - 2e-4)
+                    server.mark_resumed()
             # every request whose arrival time has passed (several, when the
             # loop was busy launching) is queued with that arrival time, so
             # the time a request waits for the loop counts in its latency
