@@ -103,3 +103,27 @@ def test_poisson_arrivals_are_reproducible_and_at_the_right_rate():
     n1 = sum(1 for _, c in a if c == 1)
     assert 500 < n0 < 700 and 230 < n1 < 370
     assert all(a[i][0] <= a[i + 1][0] for i in range(len(a) - 1))
+
+
+def test_camera_replay_in_real_time_with_idle_sleep():
+    """run_cameras against the wall clock: with the loop sleeping while
+    nothing is queued or in flight, every arrival is still served once, with
+    its own result, and nothing waits on a sleeping loop for long."""
+    import time
+    clock = time.perf_counter
+    slots = [FakeExecutor(clock, 0.0005) for _ in range(2)]
+    srv = serving.Server(slots)
+    cams = [[_frame(10 * c + k) for k in range(2)] for c in range(4)]
+    before = serving.host_counters()
+    res = serving.run_cameras(srv, cams, [200.0] * 4, duration_s=0.3, seed=5, idle_sleep=True)
+    delta = serving.counter_delta(before, serving.host_counters())
+    assert delta["involuntary_switches"] >= 0
+    arrivals = serving.poisson_arrivals([200.0] * 4, 0.3, 5)
+    assert [r.seq for r in res] == list(range(len(arrivals)))
+    k = [0] * 4
+    for r, (_, cam) in zip(res, arrivals):
+        assert r.camera == cam
+        assert int(r.quads[0]) == int(cams[cam][k[cam] % 2].sum())
+        k[cam] += 1
+    # a sleep ends 0.2 ms before the next arrival; allow for a slow host
+    assert max(r.latency_ms for r in res) < 50.0
