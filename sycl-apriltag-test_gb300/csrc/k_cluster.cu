@@ -227,42 +227,26 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     uint32_t mt, st;
     {
         const int xb = x0 + 32 * k;
-        // word k of a plane row and its neighbour-shifted forms
-        auto word = [&](int p, int row, uint32_t& L, uint32_t& C, uint32_t& R) {
-            // words k, k + 1, k + 2 of the row: three loads at the lane's
-            // offset (1.5% faster than one 16-byte load and selects)
-            const uint32_t* w3 = &planes[p][row][k];
-            const uint32_t prev = w3[0], next = w3[2];
-            C = w3[1];
-            L = __funnelshift_l(prev, C, 1);  // bit i: pixel xb + i - 1
-            R = __funnelshift_r(C, next, 1);  // bit i: pixel xb + i + 1
-        };
-        uint32_t c0L, c0, c0R, b0L, b0, b0R;
-        word(0, r, c0L, c0, c0R);
-        word(1, r, b0L, b0, b0R);
+        // The lane's tested neighbour: the same row for R (t = 0), the row
+        // below for BL, B and BR.  Bit i of its plane word is pixel
+        // xb + i + dx (dx = +1 for R and BR, -1 for BL, 0 for B): a funnel
+        // shift of words lo, lo + 1 of that plane row.
+        const int nrow = r + (t != 0 ? 1 : 0), lo = t == 1 ? k : k + 1, amt = t == 1 ? 31 : (t == 2 ? 0 : 1);
+        auto nb = [&](int p) { return __funnelshift_r(planes[p][nrow][lo], planes[p][nrow][lo + 1], amt); };
+        auto own = [&](int p) { return planes[p][r][k + 1]; };
+        const uint32_t c0 = own(0), b0 = own(1);
         uint32_t live = (y0 + r < h) ? (xb + 32 <= w ? FULL : (xb < w ? ((1u << (w - xb)) - 1u) : 0u)) : 0u;
         if (xb == 0) live &= ~1u;  // column 0 is never processed
         live &= b0 & (half ? 0xFFFF0000u : 0x0000FFFFu);
-        // the tested neighbour of test t: R (x + 1, y), BL (x - 1, y + 1),
-        // B (x, y + 1), BR (x + 1, y + 1)
-        uint32_t nc = c0R, nbg = b0R;
-        uint32_t c1L, c1, c1R, b1L, b1, b1R;
-        word(0, r + 1, c1L, c1, c1R);
-        word(1, r + 1, b1L, b1, b1R);
-        if (t == 1) { nc = c1L; nbg = b1L; }
-        if (t == 2) { nc = c1; nbg = b1; }
-        if (t == 3) { nc = c1R; nbg = b1R; }
         // BL is not emitted where the left pixel's BR covers the same pair
-        const uint32_t keep = t == 1 ? ~((c0L ^ c1) & b0L & b1) : FULL;
-        mt = (nc ^ c0) & nbg & live & keep;
+        uint32_t keep = FULL;
+        if (t == 1) {
+            const uint32_t c0L = __funnelshift_l(planes[0][r][k], c0, 1), b0L = __funnelshift_l(planes[1][r][k], b0, 1);
+            keep = ~((c0L ^ planes[0][r + 1][k + 1]) & b0L & planes[1][r + 1][k + 1]);
+        }
+        mt = (nb(0) ^ c0) & nb(1) & live & keep;
         // points whose two pixels are both labels of one published pair
-        auto of_pair = [&](int p) {
-            uint32_t L0, C0, R0, L1, C1, R1;
-            word(p, r, L0, C0, R0);
-            word(p, r + 1, L1, C1, R1);
-            return C0 & (t == 0 ? R0 : (t == 1 ? L1 : (t == 2 ? C1 : R1)));
-        };
-        st = mt & ~(of_pair(2) | of_pair(3));
+        st = mt & ~((own(2) & nb(2)) | (own(3) & nb(3)));
     }
     // Each warp lists its staged points in its own part of the staging
     // array (warp scan) and aggregates them itself, so no CTA barrier
@@ -278,7 +262,8 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     const uint32_t nst = __shfl_sync(FULL, incl, 31);
     {
         uint32_t pos = incl - ns;
-        for (uint32_t mm = st; mm; mm &= mm - 1) wst[pos++] = stage_entry(0, 32 * k + __ffs(mm) - 1, r, t, 0);
+        const uint32_t base = stage_entry(0, 32 * k, r, t, 0) - 1u;  // + ffs: pixel 32 k + ffs - 1 (mod 2^32)
+        for (uint32_t mm = st; mm; mm &= mm - 1) wst[pos++] = base + (uint32_t)__ffs(mm);
         const uint32_t nall_w = __reduce_add_sync(FULL, (uint32_t)__popc(mt));
         if (lane == 0 && nall_w) atomicAdd(&s_nall, nall_w);
     }
