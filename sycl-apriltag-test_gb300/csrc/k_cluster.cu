@@ -60,7 +60,7 @@ struct PairTableSmem {
     unsigned long long key[BP_LC];
     uint32_t cnt[BP_LC], xmin[BP_LC], xmax[BP_LC], ymin[BP_LC], ymax[BP_LC];
     int gx[BP_LC], gy[BP_LC];
-    unsigned long long pxgx[BP_LC];
+    int pxgx[BP_LC];  // a tile's sum fits 32 bits: at most 4096 points, |x| < 2^13
     uint32_t gslot[BP_LC];
 };
 
@@ -341,7 +341,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
             atomicMin(&T.ymin[ls], ymn);
             atomicMax(&T.ymax[ls], ymx);
             atomicAdd(&T.gx[ls], sgx);
-            atomicAdd(&T.pxgx[ls], (unsigned long long)(long long)spx);
+            atomicAdd(&T.pxgx[ls], spx);
         }
     }
     __syncthreads();
@@ -358,7 +358,7 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         const uint32_t gs = T.gslot[i];  // INVALID: the frame's table was full (flagged)
         if (gs == INVALID) continue;
         uint32_t old = global_flush(F, gs, T.cnt[i], T.xmin[i], T.xmax[i], T.ymin[i], T.ymax[i], T.gx[i], T.gy[i],
-                                    T.pxgx[i]);
+                                    (unsigned long long)(long long)T.pxgx[i]);
         T.gslot[i] = (old + T.cnt[i] > max_pixels) ? INVALID : gs;
         // the flush that crosses the limit publishes the pair, so that later
         // tiles skip its points (its count only grows: it stays rejected)
