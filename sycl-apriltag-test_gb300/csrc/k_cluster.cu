@@ -68,7 +68,8 @@ struct PairTableSmem {
 // atomic for keys that are already present (the common case).  *fresh is
 // set when this call inserted the key.
 __device__ __forceinline__ int local_insert(PairTableSmem& T, unsigned long long key, bool* fresh) {
-    uint32_t h = hash_key(key) & (BP_LC - 1);
+    // a 32-bit multiplicative hash of both labels (the table has 64 slots)
+    uint32_t h = (((uint32_t)key ^ ((uint32_t)(key >> 32) * 0x85EBCA6Bu)) * 0x9E3779B1u) >> 26;
     for (int p = 0; p < BP_LC; p++) {
         unsigned long long k = *(volatile unsigned long long*)&T.key[h];
         if (k == key) return (int)h;
@@ -173,11 +174,17 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     {
         constexpr int NUNIT = 2 * BP_SH, PER = (NUNIT + NW - 1) / NW;
         static_assert(NUNIT <= NW * (PER - 1) + NW - 2, "the last two warps have a unit fewer");
+        // NW is even, so a warp's units share their word k = warp & 1 and
+        // their rows are r0 + (NW / 2) j
+        static_assert(NW % 2 == 0, "units of a warp share their word");
+        const int kk = warp & 1, r0 = warp >> 1;
+        const bool xin = x0 + 32 * kk + lane < w;
+        const uint32_t* lrow = F.labels + (size_t)(y0 + r0) * w + (x0 + 32 * kk + lane);
         uint32_t lv[PER], sz[PER];
 #pragma unroll
         for (int j = 0; j < PER; j++) {
-            const int u = warp + NW * j, r = u >> 1, x = x0 + 32 * (u & 1) + lane, y = y0 + r;
-            lv[j] = (u < NUNIT && y < h && x < w) ? __ldg(F.labels + (size_t)y * w + x) : 0u;
+            const bool in = warp + NW * j < NUNIT && xin && y0 + r0 + (NW / 2) * j < h;
+            lv[j] = in ? __ldg(lrow + (size_t)j * (NW / 2) * w) : 0u;
         }
         const bool halo = warp >= NW - 2, right = warp == NW - 1;
         const int hx = right ? x0 + BP_W : x0 - 1, hy = y0 + lane;
@@ -188,8 +195,8 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         const uint32_t hs = halo ? __ldg(F.sizes + (hl & LABEL_VALUE_MASK)) : 0u;
 #pragma unroll
         for (int j = 0; j < PER; j++) {
-            const int u = warp + NW * j, r = u >> 1, k = u & 1;
-            if (u >= NUNIT) break;
+            const int r = r0 + (NW / 2) * j, k = kk;
+            if (warp + NW * j >= NUNIT) break;
             const uint32_t l = lv[j];
             lab[r][4 + 32 * k + lane] = l;
             const unsigned bc = __ballot_sync(FULL, (int)l < 0);
@@ -376,8 +383,10 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         const uint32_t e = wst[i];
         return !(e & STAGE_DIRECT) && T.gslot[(e >> 13) & 255] != INVALID;
     };
-    uint32_t nlive = 0;
-    for (uint32_t b0 = 0; b0 < nst; b0 += 32) nlive += (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, live_at(b0 + lane)));
+    // the first round's ballot is kept for the writes (most warps have one)
+    const unsigned m_first = __ballot_sync(0xFFFFFFFFu, live_at(lane));
+    uint32_t nlive = (uint32_t)__popc(m_first);
+    for (uint32_t b0 = 32; b0 < nst; b0 += 32) nlive += (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, live_at(b0 + lane)));
     if (nlive == 0) return;
     uint32_t at = 0;
     if (lane == 0) {
@@ -388,8 +397,8 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     const unsigned lt = (1u << lane) - 1u;
     for (uint32_t b0 = 0; b0 < nst; b0 += 32) {
         const uint32_t i = b0 + (uint32_t)lane;
-        const bool lv = live_at(i);
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, lv);
+        const unsigned m = b0 == 0 ? m_first : __ballot_sync(0xFFFFFFFFu, live_at(i));
+        const bool lv = (m >> lane) & 1u;
         if (lv) {
             const uint32_t e = wst[i], dst = at + (uint32_t)__popc(m & lt);
             if (dst < F.point_cap) F.points[dst] = ((unsigned long long)T.gslot[(e >> 13) & 255] << 32) | stage_packed(e, x0, y0);
