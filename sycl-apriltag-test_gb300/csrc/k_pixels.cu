@@ -70,9 +70,10 @@ __global__ void __launch_bounds__(256) k_threshold(const __grid_constant__ Frame
         uchar2 mm = make_uchar2(255, 0);
         if (tx >= 0 && tx < tw && ty >= 0 && ty < th) {
             uint32_t mn = 0xFFFFFFFFu, mx = 0;
+            const uint32_t* gp = g32 + (size_t)(ty * 4) * wpr + tx;  // the tile's first row word
 #pragma unroll
             for (int r = 0; r < 4; r++) {
-                uint32_t v = __ldg(g32 + (size_t)(ty * 4 + r) * wpr + tx);
+                uint32_t v = __ldg(gp + (size_t)r * wpr);
                 words[ey][ex][r] = v;
                 mn = __vminu4(mn, v);
                 mx = __vmaxu4(mx, v);
@@ -104,17 +105,13 @@ __global__ void __launch_bounds__(256) k_threshold(const __grid_constant__ Frame
                 make_uchar2((uint8_t)mn, (uint8_t)mx);
         uint32_t comp = (mn + (mx - mn) / 2) & 0xFF;
         bool flat = (int)(mx - mn) < min_diff;
+        // per byte: 255 above the tile's threshold, 0 at or below it, 127 in
+        // a flat tile (byte-wise unsigned compare of the four pixels at once)
+        const uint32_t comp4 = comp * 0x01010101u;
+        uint32_t* out = reinterpret_cast<uint32_t*>(F.thr) + (size_t)(ty * 4) * wpr + tx;
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-            uint32_t v = words[oy + 1][ox + 1][r], out = 0;
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                uint32_t p = (v >> (8 * b)) & 0xFF;
-                uint32_t o8 = flat ? 127u : (p > comp ? 255u : 0u);
-                out |= o8 << (8 * b);
-            }
-            reinterpret_cast<uint32_t*>(F.thr)[(size_t)(ty * 4 + r) * wpr + tx] = out;
-        }
+        for (int r = 0; r < 4; r++)
+            out[(size_t)r * wpr] = flat ? 0x7F7F7F7Fu : __vcmpgtu4(words[oy + 1][ox + 1][r], comp4);
     }
 }
 
