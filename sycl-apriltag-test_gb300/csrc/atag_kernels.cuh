@@ -174,6 +174,9 @@ __global__ void k_ccl_border_r32(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_border_edges_r8(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_border_edges_r16(const __grid_constant__ FrameSet fs);
 __global__ void k_ccl_border_edges_r32(const __grid_constant__ FrameSet fs);
+// final labelling: grid (cdiv(w / 4, CCL_FINAL_THREADS), h / 2, frames) of
+// CCL_FINAL_THREADS threads, one pair of 2x2 blocks per thread
+constexpr int CCL_FINAL_THREADS = 128;
 __global__ void k_ccl_final(const __grid_constant__ FrameSet fs);
 __global__ void k_boundaries_dense(const __grid_constant__ FrameSet fs, uint32_t min_size);
 

@@ -108,6 +108,10 @@ size_t cdiv(size_t a, size_t b) { return (a + b - 1) / b; }
 dim3 ccl_grid(size_t w, size_t h, size_t rows, size_t frames) {
     return dim3((unsigned)cdiv(w / 2, 32), (unsigned)cdiv(h / 2, rows), (unsigned)frames);
 }
+// final labelling grid: (pairs of 2x2 blocks of a row, block rows, frames)
+dim3 final_grid(size_t w, size_t h, size_t frames) {
+    return dim3((unsigned)cdiv(w / 4, CCL_FINAL_THREADS), (unsigned)(h / 2), (unsigned)frames);
+}
 
 FrameSet single(const FrameDesc& d) {
     FrameSet s;
@@ -451,8 +455,7 @@ static atag_status launch_segmentation(const FrameSet& fs, size_t max_w, size_t 
         k_ccl_border_r16<<<grid2(cdiv(border, 256), nf), 256, 0, s>>>(fs);
         LAUNCHED();
     }
-    size_t pairs = (max_w / 4) * (max_h / 2);  // k_ccl_final takes two 2x2 blocks per thread
-    k_ccl_final<<<grid2(std::min<size_t>(cdiv(pairs, 256), 8192), nf), 256, 0, s>>>(fs);
+    k_ccl_final<<<final_grid(max_w, max_h, nf), CCL_FINAL_THREADS, 0, s>>>(fs);
     LAUNCHED();
     return ATAG_OK;
 }
@@ -935,7 +938,7 @@ static atag_status launch_lane(atag_detector* det, const FrameDesc* d_table, con
         LAUNCHED();
     }
     STAGE(5);
-    k_ccl_final<<<grid2(std::min<size_t>(cdiv((mw / 4) * (mh / 2), 256), 8192), n), 256, 0, s>>>(fs);
+    k_ccl_final<<<final_grid(mw, mh, n), CCL_FINAL_THREADS, 0, s>>>(fs);
     LAUNCHED();
     STAGE(6);
     // grid (frames, tile columns, tile rows): at most 64 x 512 tiles of a

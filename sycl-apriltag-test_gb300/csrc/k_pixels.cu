@@ -607,14 +607,15 @@ __device__ __forceinline__ void ccl_border_edges_impl(const FrameSet& fs) {
 // step, so four dependent loads are in flight at once.  The forest is final
 // here; the only concurrent writes replace a parent by its root, so any
 // value read is an ancestor.
-__global__ void __launch_bounds__(256, 8) k_ccl_final(const __grid_constant__ FrameSet fs) {
-    const FrameDesc& F = fs.get(blockIdx.y);
+__global__ void __launch_bounds__(CCL_FINAL_THREADS, 2048 / CCL_FINAL_THREADS) k_ccl_final(const __grid_constant__ FrameSet fs) {
+    // grid (block pairs of a row / CCL_FINAL_THREADS, block rows, frames):
+    // the block pair from the block indices, no division
+    const FrameDesc& F = fs.get(blockIdx.z);
     const int w = F.width, h = F.height;
-    const int npx = w / 4, np = npx * (h / 2);  // block pairs (w % 4 == 0)
+    const int npx = w / 4, by = blockIdx.y, px = blockIdx.x * CCL_FINAL_THREADS + threadIdx.x;  // w % 4 == 0
     const uint32_t* par = F.scratch;
     const uint32_t cap = uf_cap_of(F);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
-        const int px = i % npx, by = i / npx;
+    if (by < h / 2 && px < npx) {
         const size_t id = (size_t)(by * 2) * w + (size_t)px * 4;
         const uint4 p4 = *reinterpret_cast<const uint4*>(F.scratch + id);
         const uint4 s4 = *reinterpret_cast<const uint4*>(F.sizes + id);

@@ -82,8 +82,8 @@ extern "C" atag_status atag_image_segmentation_noalloc(const uint8_t* thr, uint3
     count_launch();
     k_ccl_border_r16<<<dim3((unsigned)((tiles * (32 + 2 * (16 - 1)) + 255) / 256), 1), 256, 0, s>>>(fs);
     count_launch();
-    const size_t pairs = (w / 4) * (h / 2);  // two 2x2 blocks per thread
-    k_ccl_final<<<dim3((unsigned)std::min<size_t>((pairs + 255) / 256, 8192), 1), 256, 0, s>>>(fs);
+    k_ccl_final<<<dim3((unsigned)((w / 4 + CCL_FINAL_THREADS - 1) / CCL_FINAL_THREADS), (unsigned)(h / 2), 1),
+                  CCL_FINAL_THREADS, 0, s>>>(fs);
     count_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(ATAG_ERR_CUDA, cudaGetErrorString(e));
