@@ -92,8 +92,9 @@ __device__ __forceinline__ uint32_t stage_entry(int ls, int xo, int yo, int t, i
     return ((uint32_t)ls << 13) | (uint32_t)xo | ((uint32_t)yo << 6) | ((uint32_t)t << 10) | ((uint32_t)dir << 12);
 }
 __device__ __forceinline__ uint32_t stage_packed(uint32_t e, uint32_t x0, uint32_t y0) {
-    uint32_t x = x0 + (e & 63), y = y0 + ((e >> 6) & 15), t = (e >> 10) & 3, dir = (e >> 12) & 1;
-    return (x | (t << 14)) | ((y | (dir << 15)) << 16);
+    // x0 + 63 < 2^14 and y0 + 15 < 2^15: the sums leave the flag bits clear
+    const uint32_t xy = (x0 | (y0 << 16)) + (e & 63) + (((e >> 6) & 15) << 16);
+    return xy | (((e >> 10) & 3) << 14) | (((e >> 12) & 1) << 31);
 }
 
 // find_boundaries (find_boundaries.cpp:10-155) fused with the per-pair
@@ -288,9 +289,12 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
         const uint32_t i = b0 + (uint32_t)lane;
         const bool v = i < nst;
         uint32_t e = v ? wst[i] : 0u;
-        const int xo = (int)(e & 63), ro = (int)((e >> 6) & 15), t = (int)((e >> 10) & 3), c = xo + 4;
-        const int rr = ro + (t == 0 ? 0 : 1), cc = c + (t == 0 ? 1 : t - 2);
-        const uint32_t p = lab[ro][c], q = lab[rr][cc];
+        const int xo = (int)(e & 63), ro = (int)((e >> 6) & 15), t = (int)((e >> 10) & 3);
+        // the point's pixel and its tested neighbour in the label tile: R is
+        // the next word, BL, B and BR the row below (BP_SW - 1, BP_SW, BP_SW + 1)
+        static_assert(BP_SW == 72, "neighbour offsets 1, 71, 72, 73");
+        const uint32_t* pl = &lab[0][4] + ro * BP_SW + xo;
+        const uint32_t p = pl[0], q = pl[(0x49484701u >> (8 * t)) & 0xFFu];
         const uint32_t lp = p & BP_VALUE, lq = q & BP_VALUE;
         const int dir = (q & LABEL_PIXEL_MASK) > (p & LABEL_PIXEL_MASK) ? 1 : 0;
         const unsigned long long key = v ? (((unsigned long long)min(lp, lq) << 32) | max(lp, lq)) : EMPTY_KEY;
