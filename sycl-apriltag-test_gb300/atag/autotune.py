@@ -20,7 +20,7 @@ SPACE = {
     "small_ctas_per_sm": [4, 8, 12],
     "large_ctas_divisor": [1, 2, 4],
     "index_ctas_per_sm": [4, 8, 16],
-    "batch_lanes": [1, 2, 4],
+    "batch_lanes": [1, 2, 3, 4],
 }
 
 
