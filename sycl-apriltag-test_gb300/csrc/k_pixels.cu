@@ -320,7 +320,7 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
     const uint32_t lane = (uint32_t)tx;
     const unsigned sw = __ballot_sync(FULL, tx > 0 && (lw & 8u));
     const unsigned sb = __ballot_sync(FULL, tx > 0 && (lb & 8u));
-    const unsigned le = lane == 31 ? FULL : ((2u << lane) - 1u);
+    const unsigned le = (2u << lane) - 1u;  // lanes 0 .. lane (2 << 31 wraps to 0)
     const uint32_t hw = 31 - __clz(~sw & le), hb = 31 - __clz(~sb & le);  // run heads (lanes)
     const unsigned mw = le & ~((1u << hw) - 1u), mb = le & ~((1u << hb) - 1u);  // the run up to this lane
     const uint32_t row0 = (uint32_t)ty * CCL_BX;
@@ -387,10 +387,11 @@ __device__ __forceinline__ void ccl_local_impl(const FrameSet& fs) {
         if (last_b && sb_) atomicAdd(&cnt[rb], sb_);
     }
     __syncthreads();
-    auto gslot = [&](uint32_t s) {
-        uint32_t lb2 = s >> 1;
-        return (uint32_t)((by0 + lb2 / CCL_BX) * 2) * (uint32_t)w + (uint32_t)(bx0 + lb2 % CCL_BX) * 2 + (s & 1);
-    };
+    // tile slot s = 2 (row CCL_BX + col) + forest -> frame slot: the tile's
+    // first pixel plus row pixel-row pairs plus s mod 2 CCL_BX
+    static_assert(CCL_BX == 32, "a tile row is 64 slots");
+    const uint32_t tslot0 = (uint32_t)(by0 * 2) * (uint32_t)w + (uint32_t)(bx0 * 2);
+    auto gslot = [&](uint32_t s) { return tslot0 + (s >> 6) * (2u * (uint32_t)w) + (s & 63u); };
     const uint2 parents = make_uint2(gslot(rw), gslot(rb));
     if (F.edges) {
         // the edge record: tile roots of the edge blocks, with the block's
