@@ -316,7 +316,10 @@ def _serving_runs(cam_frames, W, H, seconds, overload_seconds, device):
     line = serving.latency_summary(res, seconds)
     line.update({"cameras": "4x1280x720@60 + 4x1920x1080@30", "slots": len(slots), "seconds": seconds,
                  "max_in_flight": srv.max_in_flight, "max_host_stall_ms": 1000.0 * srv.max_poll_gap,
-                 "max_poll_ms": 1000.0 * srv.max_poll_time, "host": hc, "process": "spawned child"})
+                 "max_poll_ms": 1000.0 * srv.max_poll_time, "max_launch_ms": 1000.0 * srv.max_launch_time,
+                 "max_results_ms": 1000.0 * srv.max_results_time,
+                 "max_enqueue_ms": 1000.0 * max(ex.max_enqueue_time for ex in slots),
+                 "host": hc, "process": "spawned child"})
     if overload_seconds > 0:
         srv, res, hc = run(serving.run_cameras, rates_hz=[16 * r for r in rates], duration_s=overload_seconds, seed=2)
         ov = serving.latency_summary(res, overload_seconds)
@@ -387,6 +390,20 @@ def main():
             cs = camera_specs()
             flat = list(pool.map(_render_spec, [(sp, 9000 + 10 * c + k) for c, sp in enumerate(cs) for k in range(2)]))
             cam_frames = [flat[2 * c: 2 * c + 2] for c in range(len(cs))]
+
+    # --- serving: 8 cameras (4 x 720p60, 4 x 1080p30), Poisson arrivals;
+    # then the same cameras at 16x their rates (more requests than one
+    # launch per request keeps up with: they batch), and bursts of 16
+    # simultaneous requests.  A server is a process of its own: the runs go
+    # to a spawned child process, before this process creates its CUDA
+    # context, batch detectors, graphs and pinned buffers (in a 60 s run
+    # after those legs, stalls of up to ~70 ms inside single polls appeared
+    # even in a child process).
+    serving_line = None
+    if cam_frames:
+        with concurrent.futures.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
+            serving_line = pool.submit(_serving_runs, cam_frames, W, H, args.serving_seconds,
+                                       args.overload_seconds, local_rank).result()
 
     import numpy as np
     import torch
@@ -735,18 +752,6 @@ def main():
                        "mean_decision_margin": float(dn["decision_margin"][dn["id"] >= 0].mean())
                        if (dn["id"] >= 0).any() else None}
         del detd
-
-    # --- serving: 8 cameras (4 x 720p60, 4 x 1080p30), Poisson arrivals;
-    # then the same cameras at 16x their rates (more requests than one
-    # launch per request keeps up with: they batch), and bursts of 16
-    # simultaneous requests.  A server is a process of its own: the runs go
-    # to a spawned child process, away from this process's batch detectors,
-    # graphs and pinned buffers.
-    serving_line = None
-    if cam_frames:
-        with concurrent.futures.ProcessPoolExecutor(max_workers=1, mp_context=mp.get_context("spawn")) as pool:
-            serving_line = pool.submit(_serving_runs, cam_frames, W, H, args.serving_seconds,
-                                       args.overload_seconds, local_rank).result()
 
     # --- CPU baseline (rank 0, N=1)
     cpu = None

@@ -75,6 +75,7 @@ class DetectorExecutor:
         self.max_frames = max_frames
         self.max_pixels = src_px
         self.n = 0
+        self.max_enqueue_time = 0.0  # longest detector enqueue (host side of the launches)
 
     def capacity(self):
         return self.max_frames, self.max_pixels
@@ -95,7 +96,9 @@ class DetectorExecutor:
                 views.append((off, tuple(f.shape)))
                 off += n
             dev = [self.d_in[o:o + s[0] * s[1]].view(s[0], s[1]) for o, s in views]
+            t0 = time.perf_counter()
             self.det.enqueue(dev, stream=self.stream)
+            self.max_enqueue_time = max(self.max_enqueue_time, time.perf_counter() - t0)
             self.h_stats.copy_(self.det.d_stats, non_blocking=True)
             self.h_quads.copy_(self.det.d_quads, non_blocking=True)
             self.event.record(self.stream)
@@ -161,6 +164,8 @@ class Server:
         self.max_in_flight = 0
         self.max_poll_gap = 0.0  # longest time between two polls (host stalls)
         self.max_poll_time = 0.0  # longest single poll (launches, result copies, stalls inside it)
+        self.max_launch_time = 0.0  # longest launch of one slot (copies in, detector enqueue, copies out)
+        self.max_results_time = 0.0  # longest read of one finished slot's results
         self._last_poll = None
 
     def now(self):
@@ -181,7 +186,9 @@ class Server:
                 px += frame_pixels(r.frame)
             if not take:  # a single frame larger than the slot's budget
                 raise ValueError("frame exceeds the slot pixel budget")
+            t0 = self.clock()
             ex.launch([r.frame for r in take])
+            self.max_launch_time = max(self.max_launch_time, self.clock() - t0)
             self.busy[i] = take
         self.max_in_flight = max(self.max_in_flight, sum(b is not None for b in self.busy))
 
@@ -190,7 +197,9 @@ class Server:
             reqs = self.busy[i]
             if reqs is None or not ex.done():
                 continue
+            t0 = self.clock()
             out = ex.results()
+            self.max_results_time = max(self.max_results_time, self.clock() - t0)
             t = self.now()
             for r, (quads, stats) in zip(reqs, out):
                 self.completed.append(Result(r.seq, r.camera, quads, stats, r.t_arrival, t, len(reqs)))
