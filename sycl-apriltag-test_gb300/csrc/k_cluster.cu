@@ -120,13 +120,12 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
     // labels of the tile and its halo (column c = pixel x0 + c - 4: 3 = x0 -
-    // 1, BP_W + 4 = x0 + BP_W; row BP_H is the row below the tile), and
-    // three bit planes of
-    // them: per row four words, [0] bit 31 = x0 - 1, [1] and [2] = x0 ..
-    // x0 + 63, [3] bit 0 = x0 + 64.  Plane 0: the colour bit (255 pixel),
-    // 1: the component has at least min_size pixels, 2 and 3: the label is
-    // one of the two labels of the frame's first / second pair known to be
-    // over the cluster size limit.
+    // 1, BP_W + 4 = x0 + BP_W; row BP_H is the row below the tile), and four
+    // bit planes of them: per row four words, [0] bit 31 = x0 - 1, [1] and
+    // [2] = x0 .. x0 + 63, [3] bit 0 = x0 + 64.  Plane 0: the colour bit
+    // (255 pixel), 1: the component has at least min_size pixels, 2 and 3:
+    // the label is one of the two labels of the frame's first / second pair
+    // known to be over the cluster size limit.
     __shared__ __align__(16) uint32_t lab[BP_SH][BP_SW];
     __shared__ __align__(16) uint32_t planes[4][BP_SH][4];
     __shared__ PairTableSmem T;
