@@ -51,7 +51,7 @@ __global__ void k_decimate(const __grid_constant__ FrameSet fs) {
 constexpr int TH_TX = 32, TH_TY = 16;
 constexpr int TH_EX = TH_TX + 2, TH_EY = TH_TY + 2;
 
-__global__ void __launch_bounds__(256) k_threshold(const __grid_constant__ FrameSet fs,
+__global__ void __launch_bounds__(256, 8) k_threshold(const __grid_constant__ FrameSet fs,
                                                    int min_diff, int write_extrema) {
     const FrameDesc& F = fs.get(blockIdx.y);
     const int tw = F.width / 4, th = F.height / 4;
