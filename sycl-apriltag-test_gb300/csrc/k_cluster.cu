@@ -414,14 +414,58 @@ __device__ __forceinline__ void boundaries_pairs_impl(const FrameSet& fs, uint32
 // 2. pair finalisation: sort keys, filter, cluster indices and extents
 // ---------------------------------------------------------------------------
 constexpr int PF_THREADS = 1024;
-constexpr int PF_SMEM_KEYS = 6144;
+constexpr int PF_SMEM_KEYS = 6048;  // with the scan words, under 48 KB of static shared memory
+
+// K block-wide exclusive scans at once (one set of barriers for all):
+// v[k] becomes its exclusive prefix, tot[k] the block total.  `red` holds
+// K x 33 words.
+template <int K>
+__device__ __forceinline__ void block_exclusive_scan_multi(uint32_t (&v)[K], uint32_t (*red)[33], uint32_t (&tot)[K]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    uint32_t x[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) x[k] = v[k];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x[k], o);
+            if (lane >= o) x[k] += y;
+        }
+    __syncthreads();
+    if (lane == 31)
+#pragma unroll
+        for (int k = 0; k < K; k++) red[k][wid] = x[k];
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const uint32_t s = lane < nw ? red[k][lane] : 0u;
+            uint32_t q = s;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, q, o);
+                if (lane >= o) q += y;
+            }
+            red[k][lane] = q - s;  // exclusive prefix of warp totals
+            if (lane == 31) red[k][32] = q;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        tot[k] = red[k][32];
+        v[k] = red[k][wid] + x[k] - v[k];
+    }
+}
 
 __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_constant__ FrameSet fs,
                                                                PipelineParams p, uint32_t small_max) {
     const FrameDesc& F = fs.get(blockIdx.x);
     uint32_t* status = F.counters + CNT_STATUS;
     __shared__ unsigned long long s_keys[PF_SMEM_KEYS];
-    __shared__ uint32_t red[33];
+    __shared__ uint32_t red4[4][33];
+    uint32_t* red = red4[0];
     __shared__ uint32_t s_n;
     if (threadIdx.x == 0) s_n = 0;
     __syncthreads();
@@ -461,8 +505,12 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
             pxgx = (long long)F.pair_pxgx[slot];
             keep = valid_blob(fp, cnt, bb.x, bb.y, bb.z, bb.w, gs.x, gs.y, pxgx);
         }
-        uint32_t tot_cnt, tot_keep, tot_fcnt, tot_small, tot_large, tot_fit, tot_runs;
-        uint32_t start = carry_start + block_exclusive_scan_u32(cnt, red, &tot_cnt);
+        // the scans in key order, in two rounds (which kept pairs fit
+        // depends on the first round's prefixes)
+        uint32_t s1[3] = {cnt, keep ? 1u : 0u, keep ? cnt : 0u}, t1[3];
+        block_exclusive_scan_multi<3>(s1, red4, t1);
+        const uint32_t tot_cnt = t1[0], tot_keep = t1[1], tot_fcnt = t1[2];
+        uint32_t start = carry_start + s1[0];
         if (c < C && F.pair_bounds_out) {
             // every pair's bounds in key order (stages 5-6 of the reference)
             if (c < F.pair_out_cap) {
@@ -479,15 +527,17 @@ __global__ void __launch_bounds__(PF_THREADS) k_pairs_finalize(const __grid_cons
                 atomicOr(status, ATAG_DEVFLAG_PAIR_OVERFLOW);
             }
         }
-        uint32_t cid = carry_cluster + block_exclusive_scan_u32(keep ? 1u : 0u, red, &tot_keep);
-        uint32_t fstart = carry_fstart + block_exclusive_scan_u32(keep ? cnt : 0u, red, &tot_fcnt);
+        uint32_t cid = carry_cluster + s1[1];
+        uint32_t fstart = carry_fstart + s1[2];
         const bool fits = keep && cid < F.cluster_cap && (unsigned long long)fstart + cnt <= F.cpoint_cap;
         const bool small = cnt <= small_max;
-        uint32_t js = carry_small + block_exclusive_scan_u32(fits && small ? 1u : 0u, red, &tot_small);
-        uint32_t jl = carry_large + block_exclusive_scan_u32(fits && !small ? 1u : 0u, red, &tot_large);
-        block_exclusive_scan_u32(fits ? cnt : 0u, red, &tot_fit);
-        const uint32_t run0 = carry_runs + block_exclusive_scan_u32(fits ? (cnt + CE_RUN - 1) / CE_RUN : 0u, red,
-                                                                    &tot_runs);
+        uint32_t s2[4] = {fits && small ? 1u : 0u, fits && !small ? 1u : 0u, fits ? cnt : 0u,
+                          fits ? (cnt + CE_RUN - 1) / CE_RUN : 0u}, t2[4];
+        block_exclusive_scan_multi<4>(s2, red4, t2);
+        const uint32_t tot_small = t2[0], tot_large = t2[1], tot_fit = t2[2], tot_runs = t2[3];
+        uint32_t js = carry_small + s2[0];
+        uint32_t jl = carry_large + s2[1];
+        const uint32_t run0 = carry_runs + s2[3];
         if (fits) F.cluster_work[small ? js : F.cluster_cap - 1 - jl] = cid;
         if (keep) {
             if (!fits) {
